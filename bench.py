@@ -1,0 +1,400 @@
+"""Benchmark of the GB300 adaptive embedded-RK N-body integrator.
+
+Workload (one GPU): one N = 16384 Plummer sphere (scale radius 1, velocities
+from the distribution function, seed 101), softening 0.005, the 13-stage
+Fehlberg 7(8) pair, atol = rtol = 1e-8, t in [0, 2], FP32 hi/lo pair forces
+with Kahan-compensated accumulation, FP64 state / stage combination / norm.
+A step is one adaptive attempt: 13 fused stage kernels (force + next-stage
+combination) and one controller kernel, replayed from a CUDA graph with the
+state resident in HBM.  value = accepted steps per second of device time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU implementation of the path (the
+thread-pool executor restated in oracle/, all host threads) on the same
+workload, one reference attempt per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {
+    "workload": "plummer16384_rkf78_mixed",
+    "n_particles": 16384,
+    "model": "Plummer sphere a=1, G=1, equal masses 1/N",
+    "seed": 101,
+    "softening": 0.005,
+    "tableau": "RKF78",
+    "atol": 1e-8,
+    "rtol": 1e-8,
+    "t0": 0.0,
+    "tf": 2.0,
+    "precision": "mixed",
+}
+METRIC = "accepted steps/s and pair-interactions/s at equal energy error: learned+mixed vs FP64"
+FP32_LANES_PER_SM = 128
+FLOPS_PER_INTERACTION = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) convention
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return json.load(open(p)), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU implementation (thread-pool executor, restated in
+    oracle/), one adaptive attempt per step, all host threads."""
+    if rank != 0:
+        return
+    import oracle
+    import ode_prototyping_gb300 as gb
+    W = WORKLOAD
+    n = W["n_particles"]
+    x0 = gb.ic_plummer(n, W["seed"], 1.0)
+    threads = os.cpu_count() or 1
+    ode, _ = oracle.nbody_ode(n, W["softening"], 1.0 / n)
+    sess = oracle.Session(W["tableau"], ode, x0, W["t0"], W["tf"], W["atol"], W["rtol"],
+                          threads)
+    budget_s = float(os.environ.get("GBODE_REF_BUDGET_S", "200"))
+    t_start = time.perf_counter()
+    for _ in range(max(args.warmup, 1) if args.warmup > 0 else 0):
+        sess.attempt()
+        if time.perf_counter() - t_start > budget_s / 3:
+            break
+    s0 = sess.stats()
+    done_steps, acc, t_tot = 0, 0, 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        done, a = sess.attempt()
+        t_tot += time.perf_counter() - t0
+        if done:
+            break
+        done_steps += 1
+        acc += int(a)
+        if time.perf_counter() - t_start > budget_s:
+            break
+    s1 = sess.stats()
+    rhs = s1["n_rhs"] - s0["n_rhs"]
+    value = acc / t_tot if t_tot > 0 else 0.0
+    sample = (f"{done_steps} attempts of the thread-pool reference loop restated in "
+              f"oracle/gbode_oracle.c on {threads} host threads, N={n}, {W['tableau']}")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "accepted steps/s",
+        "n_gpus": args.gpus, "steps": done_steps, "steps_requested": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_tot / max(done_steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": dict(W, precision="f64 (reference CPU path)"),
+        "pair_interactions_per_s": rhs * n * (n - 1) / t_tot if t_tot > 0 else 0.0,
+        "cpu_baseline": {"value": value, "unit": "accepted steps/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "accepted steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    sess.close()
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(n_attempts: int = 1) -> dict:
+    """Bounded sample of the same workload on the host cores: the reference's
+    thread-pool loop (restated in oracle/), one attempt after its initial-step
+    estimate, timed with the host clock."""
+    import oracle
+    import ode_prototyping_gb300 as gb
+    W = WORKLOAD
+    n = W["n_particles"]
+    threads = os.cpu_count() or 1
+    x0 = gb.ic_plummer(n, W["seed"], 1.0)
+    ode, _ = oracle.nbody_ode(n, W["softening"], 1.0 / n)
+    sess = oracle.Session(W["tableau"], ode, x0, W["t0"], W["tf"], W["atol"], W["rtol"],
+                          threads)
+    acc, t_tot = 0, 0.0
+    s0 = sess.stats()
+    for _ in range(n_attempts):
+        t0 = time.perf_counter()
+        _, a = sess.attempt()
+        t_tot += time.perf_counter() - t0
+        acc += int(a)
+    s1 = sess.stats()
+    sess.close()
+    rhs = s1["n_rhs"] - s0["n_rhs"]
+    return {"value": acc / t_tot, "unit": "accepted steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n_attempts} attempt(s) ({rhs} RHS) of the reference thread-pool loop "
+                      f"restated in oracle/, N={n} {W['tableau']}, after its initial-step "
+                      f"estimate; {t_tot:.1f} s",
+            "pair_interactions_per_s": rhs * n * (n - 1) / t_tot}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--controller", default="reference", choices=["reference", "pi", "learned"])
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    import ode_prototyping_gb300 as gb
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    W = WORKLOAD
+    n = W["n_particles"]
+    eps = W["softening"]
+    seed = W["seed"] + rank  # replicas: an independent system per GPU
+    x0 = gb.ic_plummer(n, seed, 1.0)
+    stream = torch.cuda.Stream()
+    ode = gb.NBodyODE(n, eps, 1.0 / n)
+    exe = gb.Gb300Executor(precision=W["precision"], controller=args.controller,
+                           attempts_per_sync=1)
+    S = gb.tableau(W["tableau"]).n_stages
+    it = gb.Integrator(W["tableau"], ode, exe, stream=stream)
+    e0 = gb.energy(x0, n, eps, 1.0 / n)
+    it.start(x0, W["t0"], W["tf"], W["atol"], W["rtol"])
+    it.enqueue(max(args.warmup, 0))
+    it.sync()
+    s0 = it.stats()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)  # L2 flushed between timed attempts
+            ev0[k].record(stream)
+            it.enqueue(1)
+            ev1[k].record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1))
+    it.sync()
+    s1 = it.stats()
+    accepted = s1["n_accepted"] - s0["n_accepted"]
+    attempts = s1["n_attempts"] - s0["n_attempts"]
+    rhs = s1["n_rhs"] - s0["n_rhs"]
+    xs, t_now = it.state()
+    e1 = gb.energy(xs, n, eps, 1.0 / n)
+    energy_err = abs(e1["e"] - e0["e"]) / abs(e0["e"])
+    # whole-job aggregate over ranks: accepted steps summed, time = max
+    acc_all, ms_max, rhs_all = float(accepted), ms, float(rhs)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([acc_all, rhs_all], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt)
+        tm = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        acc_all, rhs_all, ms_max = float(tt[0]), float(tt[1]), float(tm[0])
+    value = acc_all / (ms_max / 1e3)
+    pair_rate = rhs_all * n * (n - 1) / (ms_max / 1e3)
+
+    # dominant kernel: the fused stage kernel, timed alone on its stream
+    geo = it.geometry()
+    reps = 20
+    ks0 = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    ks1 = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
+    with torch.cuda.stream(stream):
+        for r in range(reps):
+            flush.fill_(r & 0xFF)
+            ks0[r].record(stream)
+            it.launch_stage(1 + r % (S - 2))
+            ks1[r].record(stream)
+    stream.synchronize()
+    k_ms = statistics.mean(a.elapsed_time(b) for a, b in zip(ks0, ks1))
+    achieved = FLOPS_PER_INTERACTION * n * (n - 1) / (k_ms / 1e3) / 1e12
+    pk, pk_kind = peaks()
+    sm_mhz_max = float(pk.get("sm_max_mhz", 2070.0))
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = n_sm * FP32_LANES_PER_SM * 2 * sm_mhz_max * 1e6 / 1e12
+    it.close()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "accepted steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {**W, "controller": args.controller, "parallelism": f"replicas{world}",
+                   "l2": "flushed between timed attempts (256 MiB write)",
+                   "step": "one adaptive attempt (13 fused stage kernels + controller kernel)"},
+        "pair_interactions_per_s": pair_rate,
+        "accepted": accepted, "attempts": attempts, "rejected": attempts - accepted,
+        "rhs_evals": rhs, "t_reached": t_now, "energy_rel_err": energy_err,
+        "clocks": clocks,
+        "gpu_launches": args.steps * (S + 1),
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "kernel": "fused_stage_kernel (mixed, one stage)",
+                     "kernel_ms": k_ms, "geometry": geo,
+                     "peak_note": f"nominal FP32 pipe: {n_sm} SMs x {FP32_LANES_PER_SM} lanes x 2"
+                                  f" x {sm_mhz_max:.0f} MHz ({pk_kind} peaks file has no FP32)",
+                     "flops_per_interaction": FLOPS_PER_INTERACTION},
+    }
+    if rank == 0:
+        line["e2e"] = e2e(gb, torch, min(args.steps, 64), x0)
+        if not args.no_fp64:
+            line["fp64_comparison"] = fp64_compare(gb, torch, x0, line)
+        if not args.no_cpu_baseline:
+            try:
+                line["cpu_baseline"] = cpu_baseline(1)
+            except Exception as ex:  # reported, not fatal
+                line["cpu_baseline"] = {"value": None, "error": repr(ex)}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def e2e(gb, torch, k_attempts: int, x0: np.ndarray) -> dict:
+    """Same metric through the public API from host memory: pinned host state
+    -> device, integrator creation + initial step + k attempts, final state
+    -> host; host clock around everything."""
+    W = WORKLOAD
+    n = W["n_particles"]
+    host = torch.from_numpy(x0).pin_memory()
+    out = torch.empty(6 * n, dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dev = host.to("cuda", non_blocking=True)
+    exe = gb.Gb300Executor(precision=W["precision"], attempts_per_sync=16)
+    it = gb.Integrator(W["tableau"], gb.NBodyODE(n, W["softening"], 1.0 / n), exe)
+    it.start(dev, W["t0"], W["tf"], W["atol"], W["rtol"])
+    it.advance(k_attempts)
+    xs, _ = it.state()
+    out.copy_(xs)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    st = it.stats()
+    it.close()
+    return {"value": st["n_accepted"] / wall, "unit": "accepted steps/s",
+            "h2d_bytes_per_step": 6 * n * 8, "d2h_bytes_per_step": 6 * n * 8,
+            "attempts": st["n_attempts"], "wall_s": wall,
+            "note": "creation, initial-step estimate and graph build inside the timed region"}
+
+
+def fp64_compare(gb, torch, x0, line, k: int = 6) -> dict:
+    """The plain FP64 GB300 path on the same workload, same tolerance, for k
+    attempts (its throughput), and the mixed path over the same k attempts
+    (energy error over the same interval)."""
+    W = WORKLOAD
+    n = W["n_particles"]
+    res = {}
+    for prec in ("f64", "mixed"):
+        stream = torch.cuda.Stream()
+        exe = gb.Gb300Executor(precision=prec, attempts_per_sync=1)
+        it = gb.Integrator(W["tableau"], gb.NBodyODE(n, W["softening"], 1.0 / n), exe,
+                           stream=stream)
+        it.start(x0, W["t0"], W["tf"], W["atol"], W["rtol"])
+        it.sync()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        s0 = it.stats()
+        a.record(stream)
+        it.enqueue(k)
+        b.record(stream)
+        stream.synchronize()
+        it.sync()
+        s1 = it.stats()
+        xs, t = it.state()
+        e0 = gb.energy(x0, n, W["softening"], 1.0 / n)
+        e1 = gb.energy(xs, n, W["softening"], 1.0 / n)
+        ms = a.elapsed_time(b)
+        res[prec] = {"accepted_steps_per_s": (s1["n_accepted"] - s0["n_accepted"]) / (ms / 1e3),
+                     "attempts": k, "t_reached": t,
+                     "energy_rel_err": abs(e1["e"] - e0["e"]) / abs(e0["e"]), "ms": ms}
+        res[prec + "_state"] = xs
+        it.close()
+    diff = (res["mixed_state"] - res["f64_state"]).abs().max().item()
+    del res["mixed_state"], res["f64_state"]
+    res["max_state_diff_mixed_vs_f64"] = diff
+    res["speedup_mixed_vs_f64"] = (res["mixed"]["accepted_steps_per_s"] /
+                                   max(res["f64"]["accepted_steps_per_s"], 1e-30))
+    return res
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,272 @@
+// force.cuh -- all-pairs softened gravity, the O(N^2) part of the right-hand
+// side of NBodyODE (src/ode/NBodyODE.hpp:68-133), owner-computes form.
+//
+// Work decomposition (one launch covers every body of one system):
+//   * a CTA owns an i-tile of BI = T / L bodies; L adjacent lanes share a body
+//     and take interleaved partners (j = j0 + l, j0 + l + L, ...);
+//   * the P CTAs of a thread-block cluster share the i-tile and split the
+//     partner range into P contiguous chunks;
+//   * partial sums are combined in a fixed order: warp shuffles over the L
+//     lanes, then cluster rank 0 adds ranks 1..P-1 read through distributed
+//     shared memory.  No atomics, bitwise reproducible run to run; with
+//     L = P = 1 each body's terms are added in ascending partner order, which
+//     is the order in which the reference's serial executor adds them (body k
+//     receives pair (m, k) for m < k, then (k, m) for m > k, and
+//     -(d/den) == (-d)/den), so the FP64 sums match it bit for bit.
+#pragma once
+
+#include "gb_internal.cuh"
+
+namespace gb {
+
+// Per-body packed j-record of the mixed-precision path: hi parts + weight,
+// then lo parts.  32 bytes, so a tile of JT bodies is one contiguous
+// 32*JT-byte block (one bulk copy).
+struct __align__(16) PackedBody {
+  float4 hw;  // hx, hy, hz, w (w = m_j, or 1 when the mass is uniform)
+  float4 lo;  // lx, ly, lz, 0
+};
+
+struct ClusterInfo {
+  int rank;
+  int size;
+  long long itile;
+};
+
+__device__ __forceinline__ ClusterInfo cluster_info() {
+  cg::cluster_group cl = cg::this_cluster();
+  ClusterInfo ci;
+  ci.rank = (int)cl.block_rank();
+  ci.size = (int)cl.num_blocks();
+  ci.itile = blockIdx.x / ci.size;
+  return ci;
+}
+
+// Partner chunk of cluster rank r: [jb, je), multiples of the tile size.
+__device__ __forceinline__ void j_chunk(long long n, int rank, int size, int jt, long long& jb,
+                                        long long& je) {
+  long long ntiles = (n + jt - 1) / jt;
+  long long per = (ntiles + size - 1) / size;
+  jb = (long long)rank * per * jt;
+  je = jb + per * jt;
+  if (jb > n) jb = n;
+  if (je > n) je = n;
+}
+
+// Reduces v over the L lanes of a body group (tree over xor offsets).
+template <int L>
+__device__ __forceinline__ double lane_reduce(double v) {
+#pragma unroll
+  for (int off = L / 2; off >= 1; off /= 2) v = dadd(v, __shfl_down_sync(0xffffffffu, v, off, L));
+  return v;
+}
+
+// Cluster-wide combine of per-body partials part[BI][3] held in each CTA's
+// shared memory; on return rank 0's part holds the totals (ranks added in
+// order 0, 1, ..., P-1).  All threads of all CTAs of the cluster must call it.
+template <int BI>
+__device__ __forceinline__ void cluster_combine(double (*part)[3], int rank, int size) {
+  cg::cluster_group cl = cg::this_cluster();
+  cl.sync();
+  if (rank == 0 && size > 1) {
+    for (int b = threadIdx.x; b < BI; b += blockDim.x) {
+      double s0 = part[b][0], s1 = part[b][1], s2 = part[b][2];
+      for (int r = 1; r < size; ++r) {
+        double(*rp)[3] = cl.map_shared_rank(part, r);
+        s0 = dadd(s0, rp[b][0]);
+        s1 = dadd(s1, rp[b][1]);
+        s2 = dadd(s2, rp[b][2]);
+      }
+      part[b][0] = s0;
+      part[b][1] = s1;
+      part[b][2] = s2;
+    }
+  }
+  cl.sync();
+}
+
+// ---------------------------------------------------------------------------
+// FP64: partial sums of one CTA over its partner chunk.  sh_pos holds 3*T
+// doubles, sh_m T doubles (per-body masses only).  Results land in part[b].
+// ---------------------------------------------------------------------------
+template <int T, int L>
+__device__ __forceinline__ void force_f64_cta(const double* __restrict__ pos, long long n,
+                                              long long i0, long long jb, long long je,
+                                              double eps2, const double* __restrict__ masses,
+                                              double* sh_pos, double* sh_m, double (*part)[3]) {
+  constexpr int BI = T / L;
+  const int b = threadIdx.x / L;
+  const int l = threadIdx.x % L;
+  const long long i = i0 + b;
+  double xi = 0.0, yi = 0.0, zi = 0.0;
+  if (i < n) {
+    xi = pos[3 * i];
+    yi = pos[3 * i + 1];
+    zi = pos[3 * i + 2];
+  }
+  double sx = 0.0, sy = 0.0, sz = 0.0;
+  for (long long j0 = jb; j0 < je; j0 += T) {
+    const int cnt = (int)min((long long)T, je - j0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * cnt; k += T) sh_pos[k] = pos[3 * j0 + k];
+    if (masses)
+      for (int k = threadIdx.x; k < cnt; k += T) sh_m[k] = masses[j0 + k];
+    __syncthreads();
+    if (i < n) {
+      for (int jj = l; jj < cnt; jj += L) {
+        const long long j = j0 + jj;
+        if (j == i) continue;
+        double ax, ay, az;
+        pair_term_f64(xi, yi, zi, sh_pos[3 * jj], sh_pos[3 * jj + 1], sh_pos[3 * jj + 2], eps2,
+                      ax, ay, az);
+        if (masses) {
+          const double mj = sh_m[jj];
+          ax = dmul(ax, mj);
+          ay = dmul(ay, mj);
+          az = dmul(az, mj);
+        }
+        sx = dadd(sx, ax);
+        sy = dadd(sy, ay);
+        sz = dadd(sz, az);
+      }
+    }
+  }
+  sx = lane_reduce<L>(sx);
+  sy = lane_reduce<L>(sy);
+  sz = lane_reduce<L>(sz);
+  if (l == 0) {
+    part[b][0] = sx;
+    part[b][1] = sy;
+    part[b][2] = sz;
+  }
+  (void)BI;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision.  Positions are stored as hi + lo FP32 parts of (x - c),
+// c a fixed reference point of the system; dx = (hj - hi) + (lj - li) keeps
+// ~2^-23 relative accuracy even for close pairs (hj - hi is exact by
+// Sterbenz's lemma when the bodies are close).  r^-3 from the SFU rsqrt.
+// Each lane sums a j-tile's terms in FP32 and Kahan-adds the tile sum into
+// its running (sum, compensation) pair; the pair is widened to FP64 for the
+// lane and cluster combine.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+template <int T, int L, int BPT>
+__device__ __forceinline__ void force_mixed_cta(const PackedBody* __restrict__ packed, long long n,
+                                                long long i0, long long jb, long long je,
+                                                float eps2, PackedBody* sh, double (*part)[3]) {
+  constexpr int BG = T / L;        // body groups per CTA
+  const int g = threadIdx.x / L;   // body group
+  const int l = threadIdx.x % L;
+  float hx[BPT], hy[BPT], hz[BPT], lx[BPT], ly[BPT], lz[BPT];
+  float sx[BPT], sy[BPT], sz[BPT], cx[BPT], cy[BPT], cz[BPT];
+#pragma unroll
+  for (int q = 0; q < BPT; ++q) {
+    const long long i = i0 + (long long)q * BG + g;
+    PackedBody pb;
+    if (i < n) {
+      pb = packed[i];
+    } else {
+      pb.hw = make_float4(0.f, 0.f, 0.f, 0.f);
+      pb.lo = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    hx[q] = pb.hw.x; hy[q] = pb.hw.y; hz[q] = pb.hw.z;
+    lx[q] = pb.lo.x; ly[q] = pb.lo.y; lz[q] = pb.lo.z;
+    sx[q] = sy[q] = sz[q] = 0.f;
+    cx[q] = cy[q] = cz[q] = 0.f;
+  }
+  constexpr int JT = T;  // bodies per j-tile
+  for (long long j0 = jb; j0 < je; j0 += JT) {
+    const int cnt = (int)min((long long)JT, je - j0);
+    __syncthreads();
+    {
+      const float4* src = reinterpret_cast<const float4*>(packed + j0);
+      float4* dst = reinterpret_cast<float4*>(sh);
+      for (int k = threadIdx.x; k < 2 * cnt; k += T) dst[k] = src[k];
+    }
+    __syncthreads();
+    float tx[BPT], ty[BPT], tz[BPT];
+#pragma unroll
+    for (int q = 0; q < BPT; ++q) tx[q] = ty[q] = tz[q] = 0.f;
+#pragma unroll 4
+    for (int jj = l; jj < cnt; jj += L) {
+      const float4 hw = sh[jj].hw;
+      const float4 lo = sh[jj].lo;
+#pragma unroll
+      for (int q = 0; q < BPT; ++q) {
+        const float dx = (hw.x - hx[q]) + (lo.x - lx[q]);
+        const float dy = (hw.y - hy[q]) + (lo.y - ly[q]);
+        const float dz = (hw.z - hz[q]) + (lo.z - lz[q]);
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+        const float rinv = rsqrtf(r2);
+        const float s = (hw.w * rinv) * (rinv * rinv);
+        tx[q] = fmaf(s, dx, tx[q]);
+        ty[q] = fmaf(s, dy, ty[q]);
+        tz[q] = fmaf(s, dz, tz[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < BPT; ++q) {
+      kahan_add(sx[q], cx[q], tx[q]);
+      kahan_add(sy[q], cy[q], ty[q]);
+      kahan_add(sz[q], cz[q], tz[q]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < BPT; ++q) {
+    double ax = dsub((double)sx[q], (double)cx[q]);
+    double ay = dsub((double)sy[q], (double)cy[q]);
+    double az = dsub((double)sz[q], (double)cz[q]);
+    ax = lane_reduce<L>(ax);
+    ay = lane_reduce<L>(ay);
+    az = lane_reduce<L>(az);
+    if (l == 0) {
+      part[q * BG + g][0] = ax;
+      part[q * BG + g][1] = ay;
+      part[q * BG + g][2] = az;
+    }
+  }
+}
+
+// Packs FP64 positions (and optional per-body masses) into PackedBody
+// records relative to the reference point c.
+__device__ __forceinline__ PackedBody pack_body(double x, double y, double z, double cx,
+                                                double cy, double cz, float w) {
+  PackedBody pb;
+  float h, lo;
+  split_hilo(dsub(x, cx), h, lo);
+  pb.hw.x = h;
+  pb.lo.x = lo;
+  split_hilo(dsub(y, cy), h, lo);
+  pb.hw.y = h;
+  pb.lo.y = lo;
+  split_hilo(dsub(z, cz), h, lo);
+  pb.hw.z = h;
+  pb.lo.z = lo;
+  pb.hw.w = w;
+  pb.lo.w = 0.f;
+  return pb;
+}
+
+// Launch geometry shared by the standalone and fused kernels.
+struct ForceGeom {
+  int T;      // threads per CTA
+  int L;      // lanes per body
+  int P;      // cluster size
+  int BPT;    // bodies per thread (mixed path)
+  long long n_itiles;
+  int bodies_per_cta() const { return (T / L) * BPT; }
+};
+
+ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling, int exact);
+int launch_cluster(const void* kernel, const ForceGeom& g, size_t smem, cudaStream_t s,
+                   void** args);
+
+}  // namespace gb

@@ -1,0 +1,1031 @@
+// integrator.cu -- device-resident adaptive embedded RK integrator for one
+// N-body system.
+//
+// Replaces RKEmbeddedParallel<BT>::integrate (src/integrator/RKEmbeddedParallel/
+// RKEmbeddedParallel.hpp:13-81) with estimate_initial_step (:170-200).  The
+// reference runs every stage, combination, norm and decision as separate
+// launches with a blocking device->host copy of the norm per attempt
+// (src/par_exec/CudaExecutor.cuh:97-125).  Here one attempt is S launches of
+// a fused kernel: stage s computes the accelerations of k_s for its i-tile
+// and, in its epilogue, the next stage state y_{s+1} = x0 + dt sum_l a[s][l]
+// k_l for the same rows (a row-local operation); the last stage forms
+// x = x0 + dt sum b k, err = dt sum (b - bt) k, the error target and the
+// scaled squares, reduces them deterministically and applies the step-size
+// controller on the device.  Attempts are captured once in a CUDA graph and
+// replayed; the host reads the controller state every `attempts_per_sync`
+// attempts.  States live in a ring of R slots so that accepting a step is an
+// index change, and accepted states can be streamed out without stalling the
+// device.
+#include <chrono>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "controller.cuh"
+#include "mlp.cuh"
+
+namespace gb {
+
+int launch_norm(const double* v, const double* s, long long n, double* partial, double* out,
+                int take_sqrt, cudaStream_t st);
+size_t norm_workspace_bytes(long long n);
+
+namespace {
+
+__device__ __forceinline__ int kslot(int l, int S, int k0slot) {
+  if (l == 0) return k0slot;
+  if (l == S - 1) return k0slot == 0 ? S - 1 : 0;
+  return l;
+}
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = dadd(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// End-of-attempt decision by one thread: acceptance (err <= 1,
+// RKEmbeddedParallel.hpp:58-62), step-size update (:65-74 or PI or learned),
+// last-step clamp (:77-79) and the loop condition t < tf (:35).
+// Shifts the step/error history as finish_attempt will (used to build the
+// learned controller's features before the decision is applied).
+__device__ __forceinline__ void preview_history(Ctrl& c, double err, bool accepted) {
+  for (int k = 2; k > 0; --k) {
+    c.dt_hist[k] = c.dt_hist[k - 1];
+    c.err_hist[k] = c.err_hist[k - 1];
+  }
+  c.dt_hist[0] = c.dt;
+  c.err_hist[0] = isfinite(err) ? err : 1e300;
+  c.last_accepted = accepted ? 1 : 0;
+}
+
+__device__ void finish_attempt(const DevTableau& tab, const FusedParams& P, Ctrl& c, double err,
+                               double learned_log_scale, bool have_learned) {
+  const double dt = c.dt;
+  c.err = err;
+  c.n_attempts += 1;
+  const bool finite = isfinite(err);
+  const bool accepted = finite && err <= 1.0;
+  if (c.learned_active) {
+    c.n_learned += 1;
+    if (!accepted) c.n_learned_rejected += 1;
+  }
+  preview_history(c, err, accepted);
+  // controller log (training data of the learned controller): the features
+  // the controller sees after this attempt, and the attempt's outcome
+  if (P.log && c.log_count < P.log_capacity) {
+    StepLog& L = P.log[c.log_count];
+    make_features(c, tab, P.n, L.feat);
+    L.log_dt = (float)log(dt);
+    L.log_err = (float)log(fmax(err, 1e-300));
+    L.accepted = accepted ? 1.f : 0.f;
+    double ideal = finite ? dt * c.safety / pow(fmax(err, 1e-300), 1.0 / (1.0 + c.q)) : dt * 0.33;
+    L.log_dt_ideal = (float)log(ideal);
+    c.log_count += 1;
+  }
+  if (!finite) {
+    c.status = GB_ERR_NOT_FINITE;
+    c.done = 1;
+    return;
+  }
+  if (accepted) {
+    c.t += dt;
+    c.cur = (c.cur + 1) % P.R;
+    P.times_ring[c.cur] = c.t;
+    c.n_accepted += 1;
+    c.px ^= 1;
+    if (c.fsal) {
+      c.k0slot = (c.k0slot == 0) ? tab.n_stages - 1 : 0;
+      c.k0_valid = 1;
+    } else {
+      c.k0_valid = 0;
+    }
+  } else {
+    c.n_rejected += 1;
+    c.k0_valid = 1;  // x0 unchanged: f(x0) is still in its slot
+  }
+  double dtn;
+  c.learned_active = 0;
+  if (c.controller == GB_CTRL_PI) {
+    dtn = pi_step(c, dt, err, accepted);
+  } else if (c.controller == GB_CTRL_LEARNED) {
+    if (accepted && have_learned) {
+      // The network proposes the next step; the embedded error estimate of
+      // that attempt still decides acceptance.
+      double scale = exp(fmin(fmax(learned_log_scale, -1.1), 1.79));  // within [0.33, 6.0]
+      if (c.reject_prev) scale = fmin(scale, 1.0);
+      dtn = dt * scale;
+      c.learned_dt = dtn;
+      c.learned_active = 1;
+      // keep the PI memory current
+      c.err_prev = fmax(err, 1.0e-4);
+      c.reject_prev = 0;
+    } else {
+      dtn = pi_step(c, dt, err, accepted);  // fallback on every rejection
+    }
+  } else {
+    dtn = reference_step(dt, err, c.safety, c.q, c.t0, c.tf);
+  }
+  c.dt = dtn;
+  if (c.t + c.dt > c.tf) c.dt = c.tf - c.t;
+  if (!(c.t < c.tf)) c.done = 1;
+  if (!c.done && c.max_attempts > 0 && c.n_attempts >= c.max_attempts) {
+    c.status = GB_ERR_BUDGET;
+    c.done = 1;
+  }
+}
+
+template <int PREC, int T, int L, int BPT>
+__global__ void __launch_bounds__(T)
+    fused_stage_kernel(const __grid_constant__ DevTableau tab,
+                       const __grid_constant__ FusedParams P, int s) {
+  constexpr int BI = (T / L) * BPT;
+  constexpr int SMEM_BODY_BYTES = PREC == GB_PREC_F64 ? 32 * T : (int)sizeof(PackedBody) * T;
+  __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
+  __shared__ double part[BI][3];
+  __shared__ double red[T];
+  Ctrl* C = P.ctrl;
+  if (C->done) return;
+  const int cur = C->cur;
+  const double dt = C->dt;
+  const int k0_valid = C->k0_valid;
+  const int k0slot = C->k0slot;
+  const int px = C->px;
+  const int S = tab.n_stages;
+  const long long n = P.n, n_var = P.n_var;
+  const double* x0 = P.ring + (long long)cur * n_var;
+  const double* ysrc = (s == 0) ? x0 : P.Y + (long long)(s & 1) * n_var;
+  const ClusterInfo ci = cluster_info();
+  const long long i0 = ci.itile * BI;
+  const bool skip_force = (s == 0 && k0_valid);
+  if (!skip_force) {
+    long long jb, je;
+    j_chunk(n, ci.rank, ci.size, T, jb, je);
+    if constexpr (PREC == GB_PREC_F64) {
+      double* sh_pos = reinterpret_cast<double*>(sh_raw);
+      double* sh_m = sh_pos + 3 * T;
+      force_f64_cta<T, L>(ysrc, n, i0, jb, je, P.eps2, P.masses, sh_pos, sh_m, part);
+    } else {
+      const PackedBody* src = (s == 0) ? P.PX + (long long)px * n : P.PY + (long long)(s & 1) * n;
+      force_mixed_cta<T, L, BPT>(src, n, i0, jb, je, P.eps2f,
+                                 reinterpret_cast<PackedBody*>(sh_raw), part);
+    }
+    cluster_combine<BI>(part, ci.rank, ci.size);
+  }
+  if (ci.rank != 0) return;
+
+  const long long nb = min((long long)BI, n - i0);
+  double* ks_s = P.ks + (long long)kslot(s, S, k0slot) * n_var;
+  const bool last = (s == S - 1);
+  double sq_acc = 0.0;
+  double amax = 0.0;
+  for (int b = threadIdx.x; b < nb; b += T) {
+    const long long i = i0 + b;
+    long long idx[6];
+    double k[6];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      idx[c] = 3 * i + c;
+      idx[3 + c] = 3 * n + 3 * i + c;
+    }
+    if (skip_force) {
+#pragma unroll
+      for (int e = 0; e < 6; ++e) k[e] = ks_s[idx[e]];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        k[c] = ysrc[idx[3 + c]];  // dx/dt = v (nbody_init_dxdt_kernel)
+        double a = part[b][c];
+        if (!P.masses) a = dmul(a, P.mass);
+        k[3 + c] = a;
+      }
+#pragma unroll
+      for (int e = 0; e < 6; ++e) ks_s[idx[e]] = k[e];
+      if (s == 0) amax = fmax(amax, sqrt(k[3] * k[3] + k[4] * k[4] + k[5] * k[5]));
+    }
+    if (!last) {
+      double yn[6];
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        double v = 0.0;
+        for (int l = 0; l <= s; ++l) {
+          const double a = tab.a[s][l];
+          if (a == 0.0) continue;
+          const double kl = (l == s) ? k[e] : P.ks[(long long)kslot(l, S, k0slot) * n_var + idx[e]];
+          v = dadd(v, dmul(a, kl));
+        }
+        yn[e] = dadd(x0[idx[e]], dmul(v, dt));
+        P.Y[(long long)((s + 1) & 1) * n_var + idx[e]] = yn[e];
+      }
+      if constexpr (PREC == GB_PREC_MIXED) {
+        const float w = P.masses ? (float)P.masses[i] : 1.0f;
+        P.PY[(long long)((s + 1) & 1) * n + i] =
+            pack_body(yn[0], yn[1], yn[2], P.cref[0], P.cref[1], P.cref[2], w);
+      }
+    } else {
+      double xn[6];
+      double* xnew = P.ring + (long long)((cur + 1) % P.R) * n_var;
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        double xv = 0.0, ev = 0.0;
+        for (int l = 0; l < S; ++l) {
+          const double bb = tab.b[l], db = tab.db[l];
+          if (bb == 0.0 && db == 0.0) continue;
+          const double kl = (l == s) ? k[e] : P.ks[(long long)kslot(l, S, k0slot) * n_var + idx[e]];
+          if (bb != 0.0) xv = dadd(xv, dmul(bb, kl));
+          if (db != 0.0) ev = dadd(ev, dmul(db, kl));
+        }
+        const double x0e = x0[idx[e]];
+        xn[e] = dadd(x0e, dmul(xv, dt));
+        const double er = dmul(ev, dt);
+        xnew[idx[e]] = xn[e];
+        const double at = P.atol ? P.atol[idx[e]] : P.atol_s;
+        const double rt = P.rtol ? P.rtol[idx[e]] : P.rtol_s;
+        const double ax = fabs(xn[e]), ax0 = fabs(x0e);
+        const double tg = dadd(at, dmul(rt, ax < ax0 ? ax0 : ax));
+        const double q = __ddiv_rn(er, tg);
+        const double sq = dmul(q, q);
+        if (P.exact) {
+          P.sq[idx[e]] = sq;
+        } else {
+          sq_acc = dadd(sq_acc, sq);
+        }
+      }
+      if constexpr (PREC == GB_PREC_MIXED) {
+        const float w = P.masses ? (float)P.masses[i] : 1.0f;
+        P.PX[(long long)(px ^ 1) * n + i] =
+            pack_body(xn[0], xn[1], xn[2], P.cref[0], P.cref[1], P.cref[2], w);
+      }
+    }
+  }
+  if (s == 0 && !skip_force) {
+    const double m = block_max(amax, red);
+    if (threadIdx.x == 0) P.aux[ci.itile] = m;
+  }
+  if (!last) return;
+  const double tile_sum = block_sum(sq_acc, red);
+  if (threadIdx.x == 0) P.partials[ci.itile] = tile_sum;
+}
+
+// End of an attempt: one CTA reduces the per-tile partial sums in tile
+// order (or, in exact mode, the per-element squares in element order, as the
+// reference's serial executor adds them), forms err = sqrt(sum / n_var)
+// (rk_norm, RKEmbeddedParallel.hpp:141-149) and runs the controller.  The
+// learned proposal is evaluated cooperatively by the whole CTA with BF16
+// weights and FP32 accumulation.
+__global__ void __launch_bounds__(256)
+    control_kernel(const __grid_constant__ DevTableau tab, const __grid_constant__ FusedParams P) {
+  constexpr int T = 256;
+  __shared__ double red[T];
+  __shared__ float feat[kIn];
+  __shared__ float h1[kHid];
+  __shared__ float outv;
+  __shared__ int sh_flag;
+  Ctrl* C = P.ctrl;
+  if (C->done) return;
+  const int S = tab.n_stages;
+  const long long n_var = P.n_var;
+  double total;
+  if (P.exact) {
+    if (threadIdx.x == 0) {
+      double v = 0.0;
+      for (long long e = 0; e < n_var; ++e) v = dadd(v, P.sq[e]);
+      red[0] = v;
+    }
+    __syncthreads();
+    total = red[0];
+    __syncthreads();
+  } else {
+    double v = 0.0;
+    for (long long k = threadIdx.x; k < P.n_itiles; k += T) v = dadd(v, P.partials[k]);
+    total = block_sum(v, red);
+  }
+  const int k0_valid = C->k0_valid;
+  double amax_all = 0.0;
+  if (!k0_valid) {
+    double v = 0.0;
+    for (long long k = threadIdx.x; k < P.n_itiles; k += T) v = fmax(v, P.aux[k]);
+    amax_all = block_max(v, red);
+  }
+  const double err = sqrt(total / (double)n_var);
+  // Learned proposal: features of the post-attempt state (thread 0), then
+  // the 16 -> 64 -> 64 -> 1 network across the CTA.
+  if (threadIdx.x == 0) {
+    Ctrl c = *C;
+    if (!k0_valid) c.max_abs_acc = amax_all;
+    const bool want = P.mlp && c.controller == GB_CTRL_LEARNED && isfinite(err) && err <= 1.0;
+    sh_flag = want ? 1 : 0;
+    if (want) {
+      Ctrl pre = c;
+      preview_history(pre, err, true);
+      make_features(pre, tab, P.n, feat);
+    }
+  }
+  __syncthreads();
+  if (sh_flag) {
+    mlp_infer_block(P.mlp, feat, h1, &outv);
+  }
+  if (threadIdx.x == 0) {
+    Ctrl c = *C;
+    if (!k0_valid) c.max_abs_acc = amax_all;
+    c.n_rhs += k0_valid ? S - 1 : S;
+    if (k0_valid) c.n_rhs_saved += 1;
+    finish_attempt(tab, P, c, err, sh_flag ? (double)outv : 0.0, sh_flag != 0);
+    *C = c;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Start-up kernels: initial step (estimate_initial_step, :170-200).
+// ---------------------------------------------------------------------------
+__global__ void target0_kernel(const double* __restrict__ x0, const double* __restrict__ atol,
+                               const double* __restrict__ rtol, double atol_s, double rtol_s,
+                               double* __restrict__ tg, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = atol ? atol[i] : atol_s;
+  const double r = rtol ? rtol[i] : rtol_s;
+  tg[i] = dadd(dmul(fabs(x0[i]), r), a);  // compute_error_target_kernel (:151-156)
+}
+
+__device__ __forceinline__ double initial_dt0(double d0, double d1) {
+  return (d0 < 1.0e-5 || d1 < 1.0e-5) ? 1.0e-6 : 0.01 * (d0 / d1);
+}
+
+__global__ void euler_kernel(const double* __restrict__ x0, const double* __restrict__ f0,
+                             const double* __restrict__ d, double* __restrict__ x1, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double dt0 = initial_dt0(d[0], d[1]);
+  x1[i] = dadd(x0[i], dmul(f0[i], dt0));  // euler_step_kernel (:158-162)
+}
+
+__global__ void diff_kernel(double* __restrict__ df, const double* __restrict__ f0, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) df[i] = dsub(df[i], f0[i]);  // difference_kernel (:164-167)
+}
+
+__global__ void pack_state_kernel(const double* __restrict__ x, const double* __restrict__ masses,
+                                  const double* __restrict__ c, long long n, PackedBody* out) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float w = masses ? (float)masses[i] : 1.0f;
+  out[i] = pack_body(x[3 * i], x[3 * i + 1], x[3 * i + 2], c[0], c[1], c[2], w);
+}
+
+__global__ void serial_norm_kernel(const double* __restrict__ v, const double* __restrict__ s,
+                                   long long n, double* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double acc = 0.0;
+  for (long long i = 0; i < n; ++i) {
+    const double q = __ddiv_rn(v[i], s[i]);
+    acc = dadd(acc, dmul(q, q));
+  }
+  *out = sqrt(acc / (double)n);
+}
+
+__global__ void centroid_state_kernel(const double* __restrict__ x, long long n, double* c_out) {
+  __shared__ double sh[3][256];
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    s0 += x[3 * i];
+    s1 += x[3 * i + 1];
+    s2 += x[3 * i + 2];
+  }
+  sh[0][threadIdx.x] = s0;
+  sh[1][threadIdx.x] = s1;
+  sh[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) {
+      for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) c_out[threadIdx.x] = sh[threadIdx.x][0] / (double)n;
+}
+
+__global__ void init_ctrl_kernel(Ctrl* C, const double* __restrict__ d, double t0, double tf,
+                                 double* times_ring, int p, int q, double safety,
+                                 int controller, double pi_beta, int fsal,
+                                 long long max_attempts) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double d0 = d[0], d1 = d[1];
+  const double dt0 = initial_dt0(d0, d1);
+  const double d2 = d[2] / dt0;
+  const double dmax = d1 < d2 ? d2 : d1;
+  double dt1;
+  if (dmax <= 1.0e-15) {
+    const double alt = dt0 * 1.0e-3;
+    dt1 = alt < 1.0e-6 ? 1.0e-6 : alt;
+  } else {
+    dt1 = pow(0.01 / dmax, 1.0 / (1.0 + p));
+  }
+  const double big = 100.0 * dt0;
+  Ctrl c;
+  memset(&c, 0, sizeof c);
+  c.t = t0;
+  c.t0 = t0;
+  c.tf = tf;
+  c.dt = dt1 < big ? dt1 : big;
+  c.dt_initial = c.dt;
+  c.safety = safety;
+  c.q = q;
+  c.controller = controller;
+  c.pi_beta = pi_beta;
+  c.pi_alpha = 1.0 / (1.0 + q) - 0.75 * pi_beta;
+  c.err_prev = 1.0e-4;
+  c.fsal = fsal;
+  c.k0_valid = 1;  // f(x0) computed for the estimate is k_0 of the first attempt
+  c.k0slot = 0;
+  c.cur = 0;
+  c.px = 0;
+  c.n_rhs = 2;
+  c.max_attempts = max_attempts;
+  for (int k = 0; k < 3; ++k) {
+    c.dt_hist[k] = c.dt;
+    c.err_hist[k] = 1.0;
+  }
+  c.done = (t0 < tf) ? 0 : 1;
+  times_ring[0] = t0;
+  *C = c;
+}
+
+__global__ void max_acc_kernel(const double* __restrict__ f, long long n, Ctrl* C) {
+  __shared__ double red[256];
+  double m = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double ax = f[3 * n + 3 * i], ay = f[3 * n + 3 * i + 1], az = f[3 * n + 3 * i + 2];
+    m = fmax(m, sqrt(ax * ax + ay * ay + az * az));
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) C->max_abs_acc = red[0];
+}
+
+unsigned blocks256(long long n) { return (unsigned)((n + 255) / 256); }
+
+// Kernel table ----------------------------------------------------------------
+template <int PREC, int T, int BPT>
+const void* pick_L(int L) {
+  switch (L) {
+    case 1: return (const void*)fused_stage_kernel<PREC, T, 1, BPT>;
+    case 2: return (const void*)fused_stage_kernel<PREC, T, 2, BPT>;
+    case 4: return (const void*)fused_stage_kernel<PREC, T, 4, BPT>;
+    case 8: return (const void*)fused_stage_kernel<PREC, T, 8, BPT>;
+    default: return nullptr;
+  }
+}
+
+const void* pick_fused(int prec, int T, int L, int BPT) {
+  if (prec == GB_PREC_F64) {
+    if (BPT != 1) return nullptr;
+    switch (T) {
+      case 64: return pick_L<GB_PREC_F64, 64, 1>(L);
+      case 128: return pick_L<GB_PREC_F64, 128, 1>(L);
+      case 256: return pick_L<GB_PREC_F64, 256, 1>(L);
+    }
+    return nullptr;
+  }
+  switch (T) {
+    case 128:
+      if (BPT == 1) return pick_L<GB_PREC_MIXED, 128, 1>(L);
+      if (BPT == 2) return pick_L<GB_PREC_MIXED, 128, 2>(L);
+      return nullptr;
+    case 256:
+      if (BPT == 1) return pick_L<GB_PREC_MIXED, 256, 1>(L);
+      if (BPT == 2) return pick_L<GB_PREC_MIXED, 256, 2>(L);
+      return nullptr;
+  }
+  return nullptr;
+}
+
+}  // namespace
+
+// Standalone RHS used by the start-up (initial step) path.
+int rhs_for_start(int prec, const double* x, double* dxdt, long long n, double softening,
+                  double mass, const double* masses, const PackedBody* packed, int exact,
+                  const gb_force_tiling* tiling, cudaStream_t s);
+
+}  // namespace gb
+
+// ---------------------------------------------------------------------------
+// Host object
+// ---------------------------------------------------------------------------
+struct gb_integrator_s {
+  gb::DevTableau tab;
+  gb_tableau htab;
+  gb_nbody_system sys;
+  gb_integrate_opts opts;
+  gb::ForceGeom geom;
+  const void* kernel = nullptr;
+  cudaStream_t user_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaEvent_t ev = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long n = 0, n_var = 0;
+  int S = 0, R = 0, A = 0;
+  // device buffers
+  gb::Ctrl* ctrl = nullptr;
+  double* ring = nullptr;
+  double* times_ring = nullptr;
+  double* ks = nullptr;
+  double* Y = nullptr;
+  gb::PackedBody* PX = nullptr;
+  gb::PackedBody* PY = nullptr;
+  double* atol = nullptr;
+  double* rtol = nullptr;
+  double* cref = nullptr;
+  double* partials = nullptr;
+  double* aux = nullptr;
+  double* sq = nullptr;
+  double* dscal = nullptr;  // initial-step norms
+  double* norm_work = nullptr;
+  double* masses = nullptr;
+  gb::StepLog* log = nullptr;
+  long long log_capacity = 0;
+  void* mlp_dev = nullptr;
+  // host
+  gb::Ctrl* hctrl = nullptr;  // pinned
+  std::vector<double> hstate;
+  long long delivered = 0;    // accepted states handed to the save callback
+  bool started = false;
+  double atol_s = 0.0, rtol_s = 0.0;
+  gb::FusedParams params;
+};
+
+namespace gb {
+namespace {
+
+int wait_event(cudaEvent_t ev, double timeout_s) {
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaEventQuery(ev);
+    if (e == cudaSuccess) return GB_OK;
+    if (e != cudaErrorNotReady) {
+      note_cuda_error(e);
+      return GB_ERR_CUDA;
+    }
+    const double el =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el > timeout_s) return GB_ERR_TIMEOUT;
+    std::this_thread::sleep_for(std::chrono::microseconds(el < 0.01 ? 5 : 200));
+  }
+}
+
+void free_all(gb_integrator_s* it) {
+  if (it->exec) cudaGraphExecDestroy(it->exec);
+  if (it->graph) cudaGraphDestroy(it->graph);
+  void* bufs[] = {it->ctrl,  it->ring, it->times_ring, it->ks,     it->Y,        it->PX,
+                  it->PY,    it->atol, it->rtol,       it->cref,   it->partials, it->aux,
+                  it->sq,    it->dscal, it->norm_work, it->masses, it->log,      it->mlp_dev};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (it->hctrl) cudaFreeHost(it->hctrl);
+  if (it->ev) cudaEventDestroy(it->ev);
+  if (it->stream && it->own_stream) cudaStreamDestroy(it->stream);
+}
+
+int launch_fused(gb_integrator_s* it, int s) {
+  void* args[] = {(void*)&it->tab, (void*)&it->params, (void*)&s};
+  GB_TRY(launch_cluster(it->kernel, it->geom, 0, it->stream, args));
+  if (s == it->S - 1) {
+    control_kernel<<<1, 256, 0, it->stream>>>(it->tab, it->params);
+    GB_CUDA_TRY(cudaGetLastError());
+  }
+  return GB_OK;
+}
+
+int build_graph(gb_integrator_s* it) {
+  GB_CUDA_TRY(cudaStreamBeginCapture(it->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = GB_OK;
+  for (int a = 0; a < it->A && rc == GB_OK; ++a)
+    for (int s = 0; s < it->S && rc == GB_OK; ++s) rc = launch_fused(it, s);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(it->stream, &g);
+  if (rc != GB_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  GB_CUDA_TRY(e);
+  it->graph = g;
+  GB_CUDA_TRY(cudaGraphInstantiate(&it->exec, g, 0));
+  return GB_OK;
+}
+
+int read_ctrl(gb_integrator_s* it) {
+  GB_CUDA_TRY(cudaMemcpyAsync(it->hctrl, it->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost,
+                              it->stream));
+  GB_CUDA_TRY(cudaEventRecord(it->ev, it->stream));
+  return wait_event(it->ev, it->opts.host_wait_timeout_s);
+}
+
+// Hands newly accepted states to the callback, in order (ring slots
+// delivered+1 .. n_accepted).
+int drain(gb_integrator_s* it, gb_save_fn save, void* user) {
+  if (!save || !it->opts.record) {
+    it->delivered = it->hctrl->n_accepted;
+    return GB_OK;
+  }
+  const long long upto = it->hctrl->n_accepted;
+  for (long long k = it->delivered + 1; k <= upto; ++k) {
+    const int slot = (int)(k % it->R);
+    double t = 0.0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&t, it->times_ring + slot, sizeof(double),
+                                cudaMemcpyDeviceToHost, it->stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(it->hstate.data(), it->ring + (long long)slot * it->n_var,
+                                it->n_var * sizeof(double), cudaMemcpyDeviceToHost, it->stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(it->stream));
+    save(user, t, it->hstate.data(), it->n_var);
+  }
+  it->delivered = upto;
+  return GB_OK;
+}
+
+}  // namespace
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system* sys,
+                                    const gb_integrate_opts* opts_in, gb_stream_t stream,
+                                    gb_integrator* out) {
+  if (!out) return GB_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  GB_TRY(check_tableau(tab));
+  if (!sys || sys->n_particles < 2 || !(sys->softening >= 0.0)) return GB_ERR_INVALID_ARGUMENT;
+  if (!sys->masses_dev && !(sys->mass > 0.0)) return GB_ERR_INVALID_ARGUMENT;
+  gb_integrate_opts opts;
+  std::memset(&opts, 0, sizeof opts);
+  if (opts_in) opts = *opts_in;
+  if (opts.precision != GB_PREC_F64 && opts.precision != GB_PREC_MIXED)
+    return GB_ERR_INVALID_ARGUMENT;
+  if (opts.precision == GB_PREC_MIXED && !(sys->softening > 0.0)) return GB_ERR_INVALID_ARGUMENT;
+  if (opts.precision == GB_PREC_MIXED && opts.exact) return GB_ERR_INVALID_ARGUMENT;
+  if (opts.controller < GB_CTRL_REFERENCE || opts.controller > GB_CTRL_LEARNED)
+    return GB_ERR_INVALID_ARGUMENT;
+  if (opts.controller == GB_CTRL_LEARNED && !opts.mlp) return GB_ERR_INVALID_ARGUMENT;
+  if (opts.attempts_per_sync <= 0) opts.attempts_per_sync = 16;
+  if (opts.attempts_per_sync > 4096) opts.attempts_per_sync = 4096;
+  if (opts.host_wait_timeout_s <= 0.0) opts.host_wait_timeout_s = 600.0;
+  if (opts.pi_beta <= 0.0) opts.pi_beta = 0.04;
+
+  auto* it = new gb_integrator_s();
+  it->htab = *tab;
+  it->tab = make_dev_tableau(*tab);
+  if (!opts.fsal) it->tab.fsal = 0;
+  it->sys = *sys;
+  it->opts = opts;
+  it->n = sys->n_particles;
+  it->n_var = 6 * it->n;
+  it->S = tab->n_stages;
+  it->A = opts.attempts_per_sync;
+  it->R = opts.record ? it->A + 2 : 2;
+  it->user_stream = as_cuda(stream);
+  it->geom = choose_geom(it->n, opts.precision, &opts.tiling, opts.exact);
+  if (opts.precision == GB_PREC_F64) it->geom.BPT = 1;
+  if (opts.precision == GB_PREC_MIXED && it->geom.T < 128) it->geom.T = 128;
+  it->geom.n_itiles = (it->n + it->geom.bodies_per_cta() - 1) / it->geom.bodies_per_cta();
+  it->kernel = pick_fused(opts.precision, it->geom.T, it->geom.L, it->geom.BPT);
+  int rc = GB_OK;
+  auto fail = [&](int code) {
+    free_all(it);
+    delete it;
+    return code;
+  };
+  if (!it->kernel) return fail(GB_ERR_UNSUPPORTED);
+  const long long n = it->n, nv = it->n_var;
+  cudaError_t e = cudaSuccess;
+#define GB_ALLOC(ptr, bytes)                                        \
+  do {                                                              \
+    e = cudaMalloc((void**)&(ptr), (bytes));                        \
+    if (e != cudaSuccess) {                                         \
+      note_cuda_error(e);                                           \
+      return fail(GB_ERR_CUDA);                                     \
+    }                                                               \
+  } while (0)
+  GB_ALLOC(it->ctrl, sizeof(Ctrl));
+  GB_ALLOC(it->ring, (size_t)it->R * nv * sizeof(double));
+  GB_ALLOC(it->times_ring, (size_t)it->R * sizeof(double));
+  GB_ALLOC(it->ks, (size_t)it->S * nv * sizeof(double));
+  GB_ALLOC(it->Y, (size_t)2 * nv * sizeof(double));
+  GB_ALLOC(it->cref, 4 * sizeof(double));
+  GB_ALLOC(it->partials, (size_t)it->geom.n_itiles * sizeof(double));
+  GB_ALLOC(it->aux, (size_t)it->geom.n_itiles * sizeof(double));
+  GB_ALLOC(it->dscal, 8 * sizeof(double));
+  GB_ALLOC(it->norm_work, norm_workspace_bytes(nv));
+  if (opts.exact) GB_ALLOC(it->sq, (size_t)nv * sizeof(double));
+  if (opts.precision == GB_PREC_MIXED) {
+    GB_ALLOC(it->PX, (size_t)2 * n * sizeof(PackedBody));
+    GB_ALLOC(it->PY, (size_t)2 * n * sizeof(PackedBody));
+  }
+  if (sys->masses_dev) {
+    GB_ALLOC(it->masses, (size_t)n * sizeof(double));
+    e = cudaMemcpy(it->masses, sys->masses_dev, n * sizeof(double), cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+      note_cuda_error(e);
+      return fail(GB_ERR_CUDA);
+    }
+  }
+  if (opts.log_steps > 0) {
+    it->log_capacity = opts.log_steps;
+    GB_ALLOC(it->log, (size_t)it->log_capacity * sizeof(StepLog));
+  }
+  if (opts.controller == GB_CTRL_LEARNED) {
+    it->mlp_dev = mlp_upload(opts.mlp, &rc);
+    if (!it->mlp_dev) return fail(rc == GB_OK ? GB_ERR_INVALID_ARGUMENT : rc);
+  }
+#undef GB_ALLOC
+  e = cudaMallocHost((void**)&it->hctrl, sizeof(Ctrl));
+  if (e == cudaSuccess) {
+    // Graphs cannot be captured on the legacy default stream: run on the
+    // caller's stream when it is a real stream, else on an owned one.
+    if (it->user_stream) {
+      it->stream = it->user_stream;
+    } else {
+      e = cudaStreamCreateWithFlags(&it->stream, cudaStreamNonBlocking);
+      it->own_stream = true;
+    }
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&it->ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMemset(it->ctrl, 0, sizeof(Ctrl));
+  if (e != cudaSuccess) {
+    note_cuda_error(e);
+    return fail(GB_ERR_CUDA);
+  }
+  std::memset(it->hctrl, 0, sizeof(Ctrl));
+  it->hstate.resize((size_t)nv);
+
+  FusedParams& P = it->params;
+  std::memset(&P, 0, sizeof P);
+  P.ctrl = it->ctrl;
+  P.ring = it->ring;
+  P.times_ring = it->times_ring;
+  P.ks = it->ks;
+  P.Y = it->Y;
+  P.PX = it->PX;
+  P.PY = it->PY;
+  P.masses = it->masses;
+  P.mass = sys->mass;
+  P.eps2 = sys->softening * sys->softening;
+  P.eps2f = (float)P.eps2;
+  P.R = it->R;
+  P.cref = it->cref;
+  P.partials = it->partials;
+  P.sq = it->sq;
+  P.aux = it->aux;
+  P.log = it->log;
+  P.log_capacity = it->log_capacity;
+  P.mlp = it->mlp_dev;
+  P.n = n;
+  P.n_var = nv;
+  P.n_itiles = it->geom.n_itiles;
+  P.exact = opts.exact;
+  P.S = it->S;
+  *out = it;
+  return GB_OK;
+}
+
+extern "C" int gb_integrator_start(gb_integrator it, const double* x0, double t0, double tf,
+                                   const double* atol_dev, const double* rtol_dev,
+                                   double atol_s, double rtol_s, gb_save_fn save, void* user) {
+  if (!it || !x0) return GB_ERR_INVALID_ARGUMENT;
+  if (!std::isfinite(t0) || !std::isfinite(tf)) return GB_ERR_INVALID_ARGUMENT;
+  if ((!atol_dev && !(atol_s >= 0.0)) || (!rtol_dev && !(rtol_s >= 0.0)))
+    return GB_ERR_INVALID_ARGUMENT;
+  const long long n = it->n, nv = it->n_var;
+  cudaStream_t s = it->stream;
+  // order after the caller's prior work on its stream
+  GB_CUDA_TRY(cudaEventRecord(it->ev, it->user_stream));
+  GB_CUDA_TRY(cudaStreamWaitEvent(s, it->ev, 0));
+  FusedParams& P = it->params;
+  if (atol_dev) {
+    if (!it->atol) GB_CUDA_TRY(cudaMalloc((void**)&it->atol, nv * sizeof(double)));
+    GB_CUDA_TRY(cudaMemcpyAsync(it->atol, atol_dev, nv * sizeof(double),
+                                cudaMemcpyDeviceToDevice, s));
+  }
+  if (rtol_dev) {
+    if (!it->rtol) GB_CUDA_TRY(cudaMalloc((void**)&it->rtol, nv * sizeof(double)));
+    GB_CUDA_TRY(cudaMemcpyAsync(it->rtol, rtol_dev, nv * sizeof(double),
+                                cudaMemcpyDeviceToDevice, s));
+  }
+  P.atol = atol_dev ? it->atol : nullptr;
+  P.rtol = rtol_dev ? it->rtol : nullptr;
+  P.atol_s = atol_s;
+  P.rtol_s = rtol_s;
+  // x0 -> ring slot 0
+  GB_CUDA_TRY(cudaMemcpyAsync(it->ring, x0, nv * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  const int prec = it->opts.precision;
+  if (prec == GB_PREC_MIXED) {
+    centroid_state_kernel<<<1, 256, 0, s>>>(it->ring, n, it->cref);
+    GB_CUDA_TRY(cudaGetLastError());
+    pack_state_kernel<<<blocks256(n), 256, 0, s>>>(it->ring, it->masses, it->cref, n, it->PX);
+    GB_CUDA_TRY(cudaGetLastError());
+  }
+  // estimate_initial_step: target -> Y[0], f0 -> ks slot 0, x1 -> Y[1],
+  // df -> ks slot 1.
+  double* tg = it->Y;
+  double* x1 = it->Y + nv;
+  double* f0 = it->ks;
+  double* df = it->ks + nv;
+  target0_kernel<<<blocks256(nv), 256, 0, s>>>(it->ring, P.atol, P.rtol, atol_s, rtol_s, tg, nv);
+  GB_CUDA_TRY(cudaGetLastError());
+  const gb_nbody_system& sys = it->sys;
+  GB_TRY(rhs_for_start(prec, it->ring, f0, n, sys.softening, sys.mass, it->masses, it->PX,
+                       it->opts.exact, &it->opts.tiling, s));
+  double* d = it->dscal;
+  if (it->opts.exact) {
+    serial_norm_kernel<<<1, 32, 0, s>>>(it->ring, tg, nv, d + 0);
+    serial_norm_kernel<<<1, 32, 0, s>>>(f0, tg, nv, d + 1);
+  } else {
+    GB_TRY(launch_norm(it->ring, tg, nv, it->norm_work, d + 0, 1, s));
+    GB_TRY(launch_norm(f0, tg, nv, it->norm_work, d + 1, 1, s));
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  euler_kernel<<<blocks256(nv), 256, 0, s>>>(it->ring, f0, d, x1, nv);
+  GB_CUDA_TRY(cudaGetLastError());
+  if (prec == GB_PREC_MIXED) {
+    pack_state_kernel<<<blocks256(n), 256, 0, s>>>(x1, it->masses, it->cref, n, it->PY);
+    GB_CUDA_TRY(cudaGetLastError());
+  }
+  GB_TRY(rhs_for_start(prec, x1, df, n, sys.softening, sys.mass, it->masses, it->PY,
+                       it->opts.exact, &it->opts.tiling, s));
+  diff_kernel<<<blocks256(nv), 256, 0, s>>>(df, f0, nv);
+  GB_CUDA_TRY(cudaGetLastError());
+  if (it->opts.exact) {
+    serial_norm_kernel<<<1, 32, 0, s>>>(df, tg, nv, d + 2);
+  } else {
+    GB_TRY(launch_norm(df, tg, nv, it->norm_work, d + 2, 1, s));
+  }
+  GB_CUDA_TRY(cudaGetLastError());
+  const int q = it->htab.p < it->htab.pt ? it->htab.p : it->htab.pt;
+  const double safety = std::pow(0.38, (1.0 / (1.0 + q)));
+  init_ctrl_kernel<<<1, 32, 0, s>>>(it->ctrl, d, t0, tf, it->times_ring, it->htab.p, q, safety,
+                                    it->opts.controller, it->opts.pi_beta, it->tab.fsal,
+                                    it->opts.max_attempts);
+  GB_CUDA_TRY(cudaGetLastError());
+  max_acc_kernel<<<1, 256, 0, s>>>(f0, n, it->ctrl);
+  GB_CUDA_TRY(cudaGetLastError());
+  if (!it->exec) GB_TRY(build_graph(it));
+  GB_TRY(read_ctrl(it));
+  it->delivered = 0;
+  it->started = true;
+  if (save && it->opts.record) {
+    GB_CUDA_TRY(cudaMemcpyAsync(it->hstate.data(), it->ring, nv * sizeof(double),
+                                cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    save(user, t0, it->hstate.data(), nv);
+  }
+  return GB_OK;
+}
+
+extern "C" int gb_integrator_enqueue(gb_integrator it, int64_t n_replays) {
+  if (!it || !it->started || n_replays < 0) return GB_ERR_INVALID_ARGUMENT;
+  for (int64_t r = 0; r < n_replays; ++r) GB_CUDA_TRY(cudaGraphLaunch(it->exec, it->stream));
+  return GB_OK;
+}
+
+extern "C" int gb_integrator_sync(gb_integrator it) {
+  if (!it) return GB_ERR_INVALID_ARGUMENT;
+  GB_TRY(read_ctrl(it));
+  GB_CUDA_TRY(cudaEventRecord(it->ev, it->stream));
+  GB_CUDA_TRY(cudaStreamWaitEvent(it->user_stream, it->ev, 0));
+  return GB_OK;
+}
+
+extern "C" int gb_integrator_advance(gb_integrator it, int64_t max_attempts, gb_save_fn save,
+                                     void* user) {
+  if (!it || !it->started) return GB_ERR_INVALID_ARGUMENT;
+  const long long start_attempts = it->hctrl->n_attempts;
+  while (!it->hctrl->done) {
+    if (max_attempts > 0 && it->hctrl->n_attempts - start_attempts >= max_attempts) break;
+    GB_CUDA_TRY(cudaGraphLaunch(it->exec, it->stream));
+    GB_TRY(read_ctrl(it));
+    GB_TRY(drain(it, save, user));
+  }
+  GB_TRY(drain(it, save, user));
+  GB_CUDA_TRY(cudaEventRecord(it->ev, it->stream));
+  GB_CUDA_TRY(cudaStreamWaitEvent(it->user_stream, it->ev, 0));
+  return it->hctrl->status;
+}
+
+extern "C" int gb_integrator_launch_stage(gb_integrator it, int32_t stage) {
+  if (!it || !it->started || stage < 0 || stage >= it->S) return GB_ERR_INVALID_ARGUMENT;
+  void* args[] = {(void*)&it->tab, (void*)&it->params, (void*)&stage};
+  return launch_cluster(it->kernel, it->geom, 0, it->stream, args);
+}
+
+extern "C" int gb_integrator_geometry(gb_integrator it, gb_force_tiling* out, int64_t* n_ctas) {
+  if (!it || !out) return GB_ERR_INVALID_ARGUMENT;
+  out->j_split = it->geom.P;
+  out->lanes = it->geom.L;
+  out->bodies_per_cta = it->geom.bodies_per_cta();
+  out->reserved = it->geom.T;
+  if (n_ctas) *n_ctas = it->geom.n_itiles * it->geom.P;
+  return GB_OK;
+}
+
+extern "C" int gb_integrator_stats(gb_integrator it, gb_integrate_stats* o) {
+  if (!it || !o) return GB_ERR_INVALID_ARGUMENT;
+  const Ctrl& c = *it->hctrl;
+  std::memset(o, 0, sizeof *o);
+  o->n_accepted = c.n_accepted;
+  o->n_rejected = c.n_rejected;
+  o->n_attempts = c.n_attempts;
+  o->n_rhs = c.n_rhs;
+  o->n_rhs_saved = c.n_rhs_saved;
+  o->t = c.t;
+  o->dt = c.dt;
+  o->dt_initial = c.dt_initial;
+  o->err_last = c.err;
+  o->interactions = (double)c.n_rhs * (double)it->n * (double)(it->n - 1);
+  o->status = c.status;
+  o->done = c.done;
+  o->n_learned_proposals = c.n_learned;
+  o->n_learned_rejected = c.n_learned_rejected;
+  return GB_OK;
+}
+
+extern "C" int gb_integrator_state(gb_integrator it, double* x_dev, double* t_host) {
+  if (!it || !it->started) return GB_ERR_INVALID_ARGUMENT;
+  GB_TRY(read_ctrl(it));
+  if (x_dev) {
+    GB_CUDA_TRY(cudaMemcpyAsync(x_dev, it->ring + (long long)it->hctrl->cur * it->n_var,
+                                it->n_var * sizeof(double), cudaMemcpyDeviceToDevice, it->stream));
+    GB_CUDA_TRY(cudaStreamSynchronize(it->stream));
+  }
+  if (t_host) *t_host = it->hctrl->t;
+  return GB_OK;
+}
+
+extern "C" int gb_integrator_destroy(gb_integrator it) {
+  if (!it) return GB_OK;
+  cudaStreamSynchronize(it->stream);
+  free_all(it);
+  delete it;
+  return GB_OK;
+}
+
+// Step log access for the learned controller's training set.
+extern "C" int gb_integrator_log(gb_integrator it, gb_step_log* host_records, int64_t capacity,
+                                 int64_t* count) {
+  if (!it || !count) return GB_ERR_INVALID_ARGUMENT;
+  GB_TRY(read_ctrl(it));
+  long long c = it->hctrl->log_count;
+  if (c > it->log_capacity) c = it->log_capacity;
+  *count = c;
+  if (host_records && capacity > 0) {
+    long long m = c < capacity ? c : capacity;
+    if (m > 0) {
+      GB_CUDA_TRY(cudaMemcpyAsync(host_records, it->log, (size_t)m * sizeof(StepLog),
+                                  cudaMemcpyDeviceToHost, it->stream));
+      GB_CUDA_TRY(cudaStreamSynchronize(it->stream));
+    }
+  }
+  return GB_OK;
+}
+
+extern "C" int gb_integrate_nbody(const gb_tableau* tab, const gb_nbody_system* sys,
+                                  const gb_integrate_opts* opts, const double* x0, double t0,
+                                  double tf, const double* atol_dev, const double* rtol_dev,
+                                  double atol_s, double rtol_s, gb_save_fn save, void* user,
+                                  double* x_final, gb_integrate_stats* stats, gb_stream_t stream) {
+  gb_integrator it = nullptr;
+  GB_TRY(gb_integrator_create(tab, sys, opts, stream, &it));
+  int rc = gb_integrator_start(it, x0, t0, tf, atol_dev, rtol_dev, atol_s, rtol_s, save, user);
+  if (rc == GB_OK) rc = gb_integrator_advance(it, 0, save, user);
+  if (rc == GB_OK || rc == GB_ERR_BUDGET || rc == GB_ERR_NOT_FINITE) {
+    if (stats) gb_integrator_stats(it, stats);
+    if (x_final) {
+      int rc2 = gb_integrator_state(it, x_final, nullptr);
+      if (rc == GB_OK) rc = rc2;
+    }
+  }
+  gb_integrator_destroy(it);
+  return rc;
+}

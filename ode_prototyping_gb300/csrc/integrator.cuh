@@ -1,0 +1,80 @@
+// integrator.cuh -- device-resident adaptive embedded RK integrator state.
+#pragma once
+
+#include "force.cuh"
+
+namespace gb {
+
+// Controller state of one system, resident in device memory.  Written only
+// by the last CTA of the final-stage kernel of an attempt (and by the start
+// kernels); every kernel reads it once at entry.
+struct Ctrl {
+  double t, dt, t0, tf;
+  double err;         // last scaled error norm
+  double err_prev;    // PI memory: last accepted error (>= 1e-4)
+  double safety;      // 0.38^(1/(1+q)) (RKEmbeddedParallel.hpp:24)
+  double dt_initial;
+  double pi_alpha, pi_beta;
+  double max_abs_acc; // max |a| over bodies in the last attempt's first stage
+  double min_r2;      // min pair separation^2 seen in the last first stage (learned features)
+  double dt_hist[3];  // last three attempted step sizes
+  double err_hist[3]; // last three error norms
+  double learned_dt;  // last learned proposal
+  long long n_accepted, n_rejected, n_attempts, n_rhs, n_rhs_saved;
+  long long max_attempts;
+  long long n_learned, n_learned_rejected;
+  long long log_count;
+  int cur;            // ring slot holding x0
+  int done;
+  int status;
+  int k0_valid;       // the k slot k0slot holds f(x0)
+  int k0slot;         // physical k slot of stage 0: 0 or S-1
+  int px;             // packed slot of x0 (mixed)
+  int reject_prev;
+  int controller;
+  int fsal;
+  int q;
+  int last_accepted;
+  int learned_active; // the current attempt uses a learned proposal
+  unsigned ticket;
+  unsigned ticket2;
+};
+
+// Log record of one attempt (learned-controller training data).
+struct StepLog {
+  float feat[16];
+  float log_dt;       // log of the attempted step
+  float log_err;      // log of the resulting scaled error
+  float accepted;
+  float log_dt_ideal; // log of the step the I-controller formula proposes
+};
+
+struct FusedParams {
+  Ctrl* ctrl;
+  double* ring;        // R * n_var states; x0 = ring + cur * n_var
+  double* times_ring;  // R times
+  double* ks;          // S * n_var stage derivatives
+  double* Y;           // 2 * n_var stage states
+  PackedBody* PX;      // 2 * n packed (x0 / x_new), mixed only
+  PackedBody* PY;      // 2 * n packed stage positions, mixed only
+  const double* atol;  // n_var or null (scalar)
+  const double* rtol;
+  double atol_s, rtol_s;
+  const double* masses;
+  double mass;
+  double eps2;
+  float eps2f;
+  int R;
+  const double* cref;  // reference point for hi/lo packing
+  double* partials;    // n_itiles
+  double* sq;          // n_var (exact mode)
+  double* aux;         // n_itiles (max |a| partials)
+  StepLog* log;        // log_capacity records or null
+  long long log_capacity;
+  const void* mlp;     // device MLP weights (learned controller) or null
+  long long n, n_var, n_itiles;
+  int exact;
+  int S;
+};
+
+}  // namespace gb

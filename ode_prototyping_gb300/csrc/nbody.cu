@@ -1,0 +1,327 @@
+// nbody.cu -- standalone right-hand-side entry points (FP64 and mixed).
+// Replaces NBodyODE<double, 6N>::operator() / acc() (src/ode/NBodyODE.hpp:31-46)
+// and its two kernels nbody_init_dxdt_kernel (:51-56) and nbody_acc_kernel
+// (:68-133), which the reference runs as one thread per unordered pair with
+// six FP64 atomicAdds; here each body's sum is owned by one lane group.
+#include "force.cuh"
+
+namespace gb {
+
+namespace {
+
+enum { kModeRhs = 0, kModeAccWrite = 1, kModeAccAdd = 2 };
+
+template <int T, int L>
+__global__ void __launch_bounds__(T) rhs_f64_kernel(const double* __restrict__ pos,
+                                                    const double* __restrict__ vel,
+                                                    double* __restrict__ out_vel,
+                                                    double* __restrict__ out_acc, long long n,
+                                                    double eps2, double mass,
+                                                    const double* __restrict__ masses, int mode) {
+  constexpr int BI = T / L;
+  __shared__ double sh_pos[3 * T];
+  __shared__ double sh_m[T];
+  __shared__ double part[BI][3];
+  const ClusterInfo ci = cluster_info();
+  const long long i0 = ci.itile * BI;
+  long long jb, je;
+  j_chunk(n, ci.rank, ci.size, T, jb, je);
+  force_f64_cta<T, L>(pos, n, i0, jb, je, eps2, masses, sh_pos, sh_m, part);
+  cluster_combine<BI>(part, ci.rank, ci.size);
+  if (ci.rank != 0) return;
+  const long long nb = min((long long)BI, n - i0);
+  for (int e = threadIdx.x; e < 3 * nb; e += T) {
+    const long long g = 3 * i0 + e;
+    double a = part[e / 3][e % 3];
+    if (!masses) a = dmul(a, mass);
+    if (mode == kModeRhs) {
+      out_vel[g] = vel[g];
+      out_acc[g] = a;
+    } else if (mode == kModeAccWrite) {
+      out_acc[g] = a;
+    } else {
+      out_acc[g] = dadd(out_acc[g], a);
+    }
+  }
+}
+
+__global__ void centroid_kernel(const double* __restrict__ pos, long long n, double* c_out) {
+  __shared__ double sh[3][1024];
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    s0 += pos[3 * i];
+    s1 += pos[3 * i + 1];
+    s2 += pos[3 * i + 2];
+  }
+  sh[0][threadIdx.x] = s0;
+  sh[1][threadIdx.x] = s1;
+  sh[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + st];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + st];
+      sh[2][threadIdx.x] += sh[2][threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    c_out[0] = sh[0][0] / (double)n;
+    c_out[1] = sh[1][0] / (double)n;
+    c_out[2] = sh[2][0] / (double)n;
+  }
+}
+
+__global__ void pack_kernel(const double* __restrict__ pos, const double* __restrict__ masses,
+                            const double* __restrict__ c, long long n, PackedBody* out) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float w = masses ? (float)masses[i] : 1.0f;
+  out[i] = pack_body(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], c[0], c[1], c[2], w);
+}
+
+template <int T, int L, int BPT>
+__global__ void __launch_bounds__(T) rhs_mixed_kernel(const PackedBody* __restrict__ packed,
+                                                      const double* __restrict__ vel,
+                                                      double* __restrict__ out_vel,
+                                                      double* __restrict__ out_acc,
+                                                      long long n, float eps2, double mass,
+                                                      int uniform_mass) {
+  constexpr int BI = (T / L) * BPT;
+  __shared__ PackedBody sh[T];
+  __shared__ double part[BI][3];
+  const ClusterInfo ci = cluster_info();
+  const long long i0 = ci.itile * BI;
+  long long jb, je;
+  j_chunk(n, ci.rank, ci.size, T, jb, je);
+  force_mixed_cta<T, L, BPT>(packed, n, i0, jb, je, eps2, sh, part);
+  cluster_combine<BI>(part, ci.rank, ci.size);
+  if (ci.rank != 0) return;
+  const long long nb = min((long long)BI, n - i0);
+  for (int e = threadIdx.x; e < 3 * nb; e += T) {
+    const long long g = 3 * i0 + e;
+    double a = part[e / 3][e % 3];
+    if (uniform_mass) a = dmul(a, mass);
+    out_vel[g] = vel[g];
+    out_acc[g] = a;
+  }
+}
+
+template <int T>
+const void* pick_f64(int L) {
+  switch (L) {
+    case 1: return (const void*)rhs_f64_kernel<T, 1>;
+    case 2: return (const void*)rhs_f64_kernel<T, 2>;
+    case 4: return (const void*)rhs_f64_kernel<T, 4>;
+    case 8: return (const void*)rhs_f64_kernel<T, 8>;
+    default: return nullptr;
+  }
+}
+
+template <int T, int BPT>
+const void* pick_mixed_L(int L) {
+  switch (L) {
+    case 1: return (const void*)rhs_mixed_kernel<T, 1, BPT>;
+    case 2: return (const void*)rhs_mixed_kernel<T, 2, BPT>;
+    case 4: return (const void*)rhs_mixed_kernel<T, 4, BPT>;
+    case 8: return (const void*)rhs_mixed_kernel<T, 8, BPT>;
+    default: return nullptr;
+  }
+}
+
+template <int T>
+const void* pick_mixed(int L, int BPT) {
+  switch (BPT) {
+    case 1: return pick_mixed_L<T, 1>(L);
+    case 2: return pick_mixed_L<T, 2>(L);
+    case 4: return pick_mixed_L<T, 4>(L);
+    default: return nullptr;
+  }
+}
+
+int validate_nbody(const void* a, const void* b, long long n, double softening, double mass,
+                   const double* masses) {
+  if (!a || !b || n < 1) return GB_ERR_INVALID_ARGUMENT;
+  if (!(softening >= 0.0) || !std::isfinite(softening)) return GB_ERR_INVALID_ARGUMENT;
+  if (!masses && !(mass > 0.0)) return GB_ERR_INVALID_ARGUMENT;
+  return GB_OK;
+}
+
+int run_f64(const double* pos, const double* vel, double* out_vel, double* out_acc, long long n,
+            double softening, double mass, const double* masses, int mode,
+            const gb_force_tiling* tiling, cudaStream_t s) {
+  ForceGeom g = choose_geom(n, GB_PREC_F64, tiling, 0);
+  const void* k = nullptr;
+  switch (g.T) {
+    case 64: k = pick_f64<64>(g.L); break;
+    case 128: k = pick_f64<128>(g.L); break;
+    case 256: k = pick_f64<256>(g.L); break;
+  }
+  if (!k) return GB_ERR_UNSUPPORTED;
+  double eps2 = softening * softening;
+  void* args[] = {(void*)&pos, (void*)&vel, (void*)&out_vel, (void*)&out_acc, (void*)&n,
+                  (void*)&eps2, (void*)&mass, (void*)&masses, (void*)&mode};
+  return launch_cluster(k, g, 0, s, args);
+}
+
+}  // namespace
+
+// Right-hand side for the integrator's start-up (initial step estimate): FP64
+// with the integrator's tiling, or mixed from an already packed state.
+int rhs_for_start(int prec, const double* x, double* dxdt, long long n, double softening,
+                  double mass, const double* masses, const PackedBody* packed, int exact,
+                  const gb_force_tiling* tiling, cudaStream_t s) {
+  if (prec == GB_PREC_F64) {
+    gb_force_tiling t = {};
+    if (tiling) t = *tiling;
+    if (exact) {
+      t.j_split = 1;
+      t.lanes = 1;
+    }
+    return run_f64(x, x + 3 * n, dxdt, dxdt + 3 * n, n, softening, mass, masses, kModeRhs, &t,
+                   s);
+  }
+  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
+  const void* k = nullptr;
+  switch (g.T) {
+    case 64: k = pick_mixed<64>(g.L, g.BPT); break;
+    case 128: k = pick_mixed<128>(g.L, g.BPT); break;
+    case 256: k = pick_mixed<256>(g.L, g.BPT); break;
+  }
+  if (!k) return GB_ERR_UNSUPPORTED;
+  const double* vel = x + 3 * n;
+  double* out_vel = dxdt;
+  double* out_acc = dxdt + 3 * n;
+  float eps2 = (float)(softening * softening);
+  int uniform = masses ? 0 : 1;
+  void* args[] = {(void*)&packed, (void*)&vel,  (void*)&out_vel, (void*)&out_acc,
+                  (void*)&n,      (void*)&eps2, (void*)&mass,    (void*)&uniform};
+  return launch_cluster(k, g, 0, s, args);
+}
+
+int launch_cluster(const void* kernel, const ForceGeom& g, size_t smem, cudaStream_t s,
+                   void** args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(g.n_itiles * g.P), 1, 1);
+  cfg.blockDim = dim3((unsigned)g.T, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)g.P;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (g.P > 8) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  }
+  GB_CUDA_TRY(cudaLaunchKernelExC(&cfg, kernel, args));
+  return GB_OK;
+}
+
+ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling, int exact) {
+  ForceGeom g;
+  g.T = 128;
+  g.L = 1;
+  g.P = 1;
+  g.BPT = 1;
+  const int sms = num_sms();
+  if (exact) {
+    g.L = 1;
+    g.P = 1;
+  } else if (precision == GB_PREC_F64) {
+    // Aim for ~8 resident warps per SM over the whole grid.
+    long long want = (long long)sms * 8 * 32;
+    long long lp = (want + n - 1) / n;
+    int P = 1;
+    while (P < 8 && P < lp) P *= 2;
+    int L = 1;
+    while (L < 4 && (long long)P * L < lp) L *= 2;
+    g.P = P;
+    g.L = L;
+  } else {
+    g.BPT = 2;
+    // ~16 warps per SM, each lane pair-loop at least ~256 partners long.
+    long long want = (long long)sms * 16 * 32 * g.BPT;
+    long long lp = (want + n - 1) / n;
+    int P = 1;
+    while (P < 8 && P < lp && n / (2 * P) >= 256) P *= 2;
+    int L = 1;
+    while (L < 4 && (long long)P * L < lp && n / (2 * P * L) >= 128) L *= 2;
+    g.P = P;
+    g.L = L;
+  }
+  if (tiling) {
+    if (tiling->j_split > 0) g.P = tiling->j_split;
+    if (tiling->lanes > 0) g.L = tiling->lanes;
+    if (tiling->bodies_per_cta > 0) {
+      // bodies per CTA = (T / L) * BPT
+      int t = tiling->bodies_per_cta * g.L / g.BPT;
+      g.T = t <= 64 ? 64 : (t <= 128 ? 128 : 256);
+    }
+  }
+  const long long per_cta = g.bodies_per_cta();
+  g.n_itiles = (n + per_cta - 1) / per_cta;
+  return g;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" int gb_nbody_rhs_f64(const double* x, double* dxdt, int64_t n, double softening,
+                                double mass, const double* masses, const gb_force_tiling* tiling,
+                                gb_stream_t stream) {
+  GB_TRY(validate_nbody(x, dxdt, n, softening, mass, masses));
+  return run_f64(x, x + 3 * n, dxdt, dxdt + 3 * n, n, softening, mass, masses, kModeRhs, tiling,
+                 as_cuda(stream));
+}
+
+extern "C" int gb_nbody_acc_f64(const double* pos, double* acc, int64_t n, double softening,
+                                double mass, const double* masses, int32_t accumulate,
+                                const gb_force_tiling* tiling, gb_stream_t stream) {
+  GB_TRY(validate_nbody(pos, acc, n, softening, mass, masses));
+  return run_f64(pos, nullptr, nullptr, acc, n, softening, mass, masses,
+                 accumulate ? kModeAccAdd : kModeAccWrite, tiling, as_cuda(stream));
+}
+
+extern "C" size_t gb_nbody_mixed_workspace_bytes(int64_t n) {
+  if (n < 1) return 0;
+  // packed bodies + reference point (3 doubles), 256-byte aligned pieces
+  size_t packed = ((size_t)n * sizeof(PackedBody) + 255) / 256 * 256;
+  return packed + 256;
+}
+
+extern "C" int gb_nbody_rhs_mixed(const double* x, double* dxdt, int64_t n, double softening,
+                                  double mass, const double* masses, void* work,
+                                  const gb_force_tiling* tiling, gb_stream_t stream) {
+  GB_TRY(validate_nbody(x, dxdt, n, softening, mass, masses));
+  if (!work || (reinterpret_cast<uintptr_t>(work) & 15u)) return GB_ERR_INVALID_ARGUMENT;
+  if (!(softening > 0.0)) return GB_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = as_cuda(stream);
+  PackedBody* packed = reinterpret_cast<PackedBody*>(work);
+  size_t packed_bytes = ((size_t)n * sizeof(PackedBody) + 255) / 256 * 256;
+  double* c = reinterpret_cast<double*>(reinterpret_cast<char*>(work) + packed_bytes);
+  centroid_kernel<<<1, 1024, 0, s>>>(x, n, c);
+  GB_CUDA_TRY(cudaGetLastError());
+  pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, masses, c, n, packed);
+  GB_CUDA_TRY(cudaGetLastError());
+  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
+  const void* k = nullptr;
+  switch (g.T) {
+    case 64: k = pick_mixed<64>(g.L, g.BPT); break;
+    case 128: k = pick_mixed<128>(g.L, g.BPT); break;
+    case 256: k = pick_mixed<256>(g.L, g.BPT); break;
+  }
+  if (!k) return GB_ERR_UNSUPPORTED;
+  const double* vel = x + 3 * n;
+  double* out_vel = dxdt;
+  double* out_acc = dxdt + 3 * n;
+  float eps2 = (float)(softening * softening);
+  int uniform = masses ? 0 : 1;
+  long long nn = n;
+  void* args[] = {(void*)&packed, (void*)&vel,  (void*)&out_vel, (void*)&out_acc,
+                  (void*)&nn,     (void*)&eps2, (void*)&mass,    (void*)&uniform};
+  return launch_cluster(k, g, 0, s, args);
+}

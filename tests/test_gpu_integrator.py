@@ -1,0 +1,165 @@
+"""GPU parity of the device-resident adaptive integrator against the
+reference's golden values, the reference's own runs (fixtures) and the live
+oracle.  Bars: same accepted-step count, final state within 10x the
+tolerance (bitwise where stated)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(GOLDEN, "reference_goldens.json")))
+
+
+def run(gb, tab, n, soft, mass, x0, t0, tf, tol, **exe_kw):
+    exe = gb.Gb300Executor(**exe_kw)
+    ode = gb.NBodyODE(n, soft, mass)
+    out = gb.RawOutput()
+    st = gb.RKEmbeddedParallel(tab).integrate(x0, t0, tf, tol, tol, ode, out, exe)
+    return np.array(out.times()), np.array(out.states()), st
+
+
+@pytest.mark.parametrize("exe_kw", [{}, {"exact": True}, {"fsal": False},
+                                    {"attempts_per_sync": 1}, {"attempts_per_sync": 64}])
+def test_five_body_rkf78_golden(gb, torch_cuda, exe_kw):
+    """RKF78NBodyConsistencyTest (SingleThreadedRKEmbeddedTest.cpp:306-340) with
+    the CUDA executor's tolerances (CudaRKEmbeddedTest.cu:309-354)."""
+    P = GOLD["problems"]["nbody5"]
+    case = GOLD["cases"]["RKF78NBodyConsistencyTest"]
+    times, states, st = run(gb, "RKF78", 5, 0.0, 1.0, np.array(P["x0"]), P["t0"], P["tf"],
+                            P["tol"], **exe_kw)
+    assert len(times) == case["n_saved"] == 172
+    tol = P["tol"]
+    mid_tol = 1.657666 * tol * len(times) / 2
+    assert times[0] == 0.0 and times[-1] == 6.3
+    assert times[len(times) // 2] == pytest.approx(3.1699354066499978, abs=mid_tol)
+    np.testing.assert_allclose(states[-1][[0, 3, 6, 9, 12]],
+                               [1.6573213121279662, 0.46802604979077689, -1.2481480178176445,
+                                -1.2883624086182086, 0.41116306451711232], atol=tol, rtol=0)
+    assert st["n_accepted"] == 171
+
+
+def test_spinning_cube_rkf78_golden(gb, orc, torch_cuda):
+    """RKF78SpinningCubeNBodyTest (SingleThreadedRKEmbeddedTest.cpp:342-382) with
+    CudaRKEmbeddedTest.cu:356-403's 10*DBL_EPSILON tolerance."""
+    n = 1024
+    x0 = orc.spinning_cube(n, 1.0, 0)
+    soft = 4.0 / np.sqrt(n)
+    times, states, _ = run(gb, "RKF78", n, soft, 1.0, x0, 0.0, np.sqrt(1.0 / n), soft)
+    assert len(times) == 4
+    eps10 = 10 * np.finfo(float).eps
+    assert times[-1] == 0.03125
+    assert times[2] == pytest.approx(0.0099564200160493655, abs=eps10)
+    idx = [0, n // 4, n // 2, 3 * n // 4]
+    np.testing.assert_allclose(states[2][idx], [0.36755281580363885, 0.85638183296447723,
+                                                0.41417946857300797, 0.028148414608021005],
+                               atol=eps10, rtol=0)
+    np.testing.assert_allclose(states[-1][idx], [0.16121502269618729, 0.71404096847054921,
+                                                 0.59500181799963803, 0.42875743462583493],
+                               atol=eps10, rtol=0)
+
+
+@pytest.mark.parametrize("tag", ["ball64_dopri5", "ball64_rkf78", "plummer256_rkf78",
+                                 "config1_ball1024_dopri5"])
+@pytest.mark.parametrize("exact", [False, True])
+def test_matches_reference_runs(gb, torch_cuda, tag, exact):
+    path = os.path.join(GOLDEN, f"nbody_{tag}.npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture missing")
+    d = np.load(path)
+    n, soft, mass, t0, tf, tol = d["meta"]
+    n = int(n)
+    times, states, st = run(gb, str(d["tableau"]), n, soft, mass, d["x0"], t0, tf, tol,
+                            exact=exact)
+    assert len(times) == len(d["times"]), (len(times), len(d["times"]))
+    assert np.max(np.abs(states[-1] - d["final"])) <= 10 * tol
+    np.testing.assert_allclose(times, d["times"], rtol=0, atol=10 * tol)
+
+
+@pytest.mark.parametrize("n,tab,seed", [(48, "DOPRI5", 1), (100, "RKF78", 2), (33, "RKF45", 3),
+                                        (70, "DVERK", 4), (20, "HE21", 5)])
+def test_matches_live_oracle(gb, orc, torch_cuda, n, tab, seed):
+    x0 = gb.ic_plummer(n, seed)
+    soft, tol, tf = 0.05, 1e-8, 0.3 if tab != "HE21" else 0.02
+    ode, _ = orc.nbody_ode(n, soft, 1.0 / n)
+    r = orc.integrate(tab, ode, x0, 0.0, tf, tol, tol, capacity=1 << 16)
+    times, states, _ = run(gb, tab, n, soft, 1.0 / n, x0, 0.0, tf, tol)
+    assert len(times) == len(r.times)
+    assert np.max(np.abs(states[-1] - r.states[-1])) <= 10 * tol
+
+
+def test_fsal_is_bit_identical(gb, torch_cuda):
+    n = 200
+    x0 = gb.ic_uniform_ball(n, 9, 0.1)
+    a = run(gb, "DOPRI5", n, 0.02, 1.0 / n, x0, 0.0, 0.2, 1e-9, fsal=True)
+    b = run(gb, "DOPRI5", n, 0.02, 1.0 / n, x0, 0.0, 0.2, 1e-9, fsal=False)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    assert a[2]["n_rhs"] < b[2]["n_rhs"]
+    assert a[2]["n_rhs_saved"] > 0
+
+
+def test_vector_tolerances_match_scalar(gb, torch_cuda):
+    n = 64
+    x0 = gb.ic_plummer(n, 3)
+    exe = gb.Gb300Executor()
+    ode = gb.NBodyODE(n, 0.05, 1.0 / n)
+    o1, o2 = gb.RawOutput(), gb.RawOutput()
+    gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, 0.2, 1e-9, 1e-9, ode, o1, exe)
+    tv = np.full(6 * n, 1e-9)
+    gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, 0.2, tv, tv, ode, o2, exe)
+    np.testing.assert_array_equal(np.array(o1.states()), np.array(o2.states()))
+
+
+def test_mixed_precision_integrator(gb, torch_cuda):
+    n = 1024
+    x0 = gb.ic_uniform_ball(n, 1, 0.1)
+    tol = 1e-9
+    t64, s64, st64 = run(gb, "DOPRI5", n, 0.01, 1.0 / n, x0, 0.0, 0.1, tol)
+    tmx, smx, stmx = run(gb, "DOPRI5", n, 0.01, 1.0 / n, x0, 0.0, 0.1, tol, precision="mixed")
+    assert abs(len(tmx) - len(t64)) <= max(2, len(t64) // 20)
+    assert np.max(np.abs(smx[-1] - s64[-1])) <= 1e-6
+
+
+def test_budget_and_nonfinite_status(gb, torch_cuda):
+    n = 32
+    x0 = gb.ic_plummer(n, 1)
+    exe = gb.Gb300Executor(max_attempts=5)
+    it = gb.Integrator("DOPRI5", gb.NBodyODE(n, 0.05, 1.0 / n), exe)
+    it.start(x0, 0.0, 10.0, 1e-12, 1e-12)
+    assert it.advance() == gb.GB_ERR_BUDGET
+    assert it.stats()["n_attempts"] == 5
+    it.close()
+    bad = x0.copy()
+    bad[7] = np.nan
+    it = gb.Integrator("DOPRI5", gb.NBodyODE(n, 0.05, 1.0 / n), gb.Gb300Executor())
+    it.start(bad, 0.0, 1.0, 1e-9, 1e-9)
+    assert it.advance() == gb.GB_ERR_NOT_FINITE
+    it.close()
+
+
+def test_pi_controller_runs(gb, torch_cuda):
+    n = 256
+    x0 = gb.ic_plummer(n, 6)
+    t_ref, s_ref, st_ref = run(gb, "DOPRI5", n, 0.02, 1.0 / n, x0, 0.0, 0.3, 1e-9)
+    t_pi, s_pi, st_pi = run(gb, "DOPRI5", n, 0.02, 1.0 / n, x0, 0.0, 0.3, 1e-9, controller="pi")
+    assert t_pi[-1] == pytest.approx(0.3)
+    assert np.max(np.abs(s_pi[-1] - s_ref[-1])) <= 1e-7
+
+
+def test_enqueue_and_state(gb, torch_cuda):
+    n = 128
+    x0 = gb.ic_plummer(n, 2)
+    it = gb.Integrator("RKF78", gb.NBodyODE(n, 0.02, 1.0 / n), gb.Gb300Executor())
+    it.start(x0, 0.0, 0.1, 1e-9, 1e-9)
+    it.enqueue(2)
+    it.sync()
+    s = it.stats()
+    assert s["n_attempts"] >= 1
+    x, t = it.state()
+    assert t == s["t"] and x.shape[0] == 6 * n
+    it.close()

@@ -1,0 +1,142 @@
+"""GPU parity of the N-body right-hand side against the oracle (reference
+restatement) and the reference's own outputs (fixtures)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _x(n, seed, spread=1.0):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(6 * n) * spread
+    return x
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("n,soft", [(2, 0.1), (5, 0.0), (64, 0.05), (1000, 0.01), (1024, 0.01),
+                                    (1031, 0.2)])
+def test_rhs_f64_serial_tiling_is_bitwise_reference(gb, orc, torch_cuda, n, soft):
+    """j_split = lanes = 1: every body sums its terms in ascending partner
+    order with IEEE operations -- identical to the serial executor."""
+    x = _x(n, n)
+    mass = 1.0 / n
+    ode, _ = orc.nbody_ode(n, soft, mass)
+    ref = orc.rhs(ode, x)
+    got = gb.nbody_rhs_f64(x, n, soft, mass, tile=gb.tiling(1, 1, 0)).cpu().numpy()
+    np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("P,L,B", [(0, 0, 0), (2, 1, 0), (4, 2, 0), (8, 4, 0), (8, 8, 64),
+                                   (1, 4, 32), (2, 2, 256)])
+def test_rhs_f64_tilings_within_1e12(gb, orc, torch_cuda, P, L, B):
+    n, soft = 1531, 0.01
+    x = _x(n, 7)
+    ode, _ = orc.nbody_ode(n, soft, 1.0 / n)
+    ref = orc.rhs(ode, x)
+    got = gb.nbody_rhs_f64(x, n, soft, 1.0 / n, tile=gb.tiling(P, L, B)).cpu().numpy()
+    acc_g, acc_r = got[3 * n:].reshape(-1, 3), ref[3 * n:].reshape(-1, 3)
+    # the benchmark spec bound: accelerations agree to <= 1e-12 relative
+    rel = np.linalg.norm(acc_g - acc_r, axis=1) / np.linalg.norm(acc_r, axis=1)
+    assert rel.max() <= 1e-12, rel.max()
+    np.testing.assert_array_equal(got[: 3 * n], ref[: 3 * n])
+
+
+def test_rhs_f64_deterministic(gb, torch_cuda):
+    n = 2048
+    x = _x(n, 3)
+    a = gb.nbody_rhs_f64(x, n, 0.01, 1.0 / n).cpu().numpy()
+    b = gb.nbody_rhs_f64(x, n, 0.01, 1.0 / n).cpu().numpy()
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("tag", ["ball64_dopri5", "plummer256_rkf78", "config1_ball1024_dopri5"])
+def test_rhs_f64_equals_reference_fixture(gb, torch_cuda, tag):
+    path = os.path.join(GOLDEN, f"nbody_{tag}.npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture missing")
+    d = np.load(path)
+    n, soft, mass = int(d["meta"][0]), d["meta"][1], d["meta"][2]
+    got = gb.nbody_rhs_f64(d["x0"], n, soft, mass, tile=gb.tiling(1, 1, 0)).cpu().numpy()
+    np.testing.assert_array_equal(got, d["rhs"])
+
+
+def test_rhs_f64_per_body_masses(gb, orc, torch_cuda):
+    n = 300
+    x = _x(n, 9)
+    m = np.random.default_rng(1).uniform(0.5, 2.0, n) / n
+    ode, keep = orc.nbody_ode(n, 0.02, masses=m)
+    ref = orc.rhs(ode, x)
+    mt = gb.to_device(m)
+    got = gb.nbody_rhs_f64(x, n, 0.02, masses=mt, tile=gb.tiling(1, 1, 0)).cpu().numpy()
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_acc_write_and_accumulate(gb, orc, torch_cuda):
+    n = 129
+    x = _x(n, 4)
+    ode, _ = orc.nbody_ode(n, 0.1, 1.0)
+    ref = orc.rhs(ode, x)[3 * n:]
+    acc = gb.nbody_acc_f64(x[: 3 * n], n, 0.1, 1.0, tile=gb.tiling(1, 1, 0))
+    np.testing.assert_array_equal(acc.cpu().numpy(), ref)
+    gb.nbody_acc_f64(x[: 3 * n], n, 0.1, 1.0, accumulate=True, out=acc, tile=gb.tiling(1, 1, 0))
+    np.testing.assert_array_equal(acc.cpu().numpy(), 2 * ref)
+
+
+@pytest.mark.parametrize("n,soft,gen", [(1024, 0.01, "ball"), (4096, 0.005, "plummer"),
+                                        (16384, 0.005, "plummer"), (3001, 0.003, "binary")])
+def test_rhs_mixed_within_1e6_of_fp64(gb, torch_cuda, n, soft, gen):
+    if gen == "ball":
+        x = gb.ic_uniform_ball(n, 1, 0.1)
+    elif gen == "plummer":
+        x = gb.ic_plummer(n, 2)
+    else:
+        x = gb.ic_binary_plummer(n, 3, 0.1, 1e-3, 1e-2)
+    ref = gb.nbody_rhs_f64(x, n, soft, 1.0 / n).cpu().numpy()
+    got = gb.nbody_rhs_mixed(x, n, soft, 1.0 / n).cpu().numpy()
+    np.testing.assert_array_equal(got[: 3 * n], ref[: 3 * n])
+    a_g, a_r = got[3 * n:].reshape(-1, 3), ref[3 * n:].reshape(-1, 3)
+    # normwise relative error of the acceleration field
+    assert _rel(a_g, a_r) <= 1e-6, _rel(a_g, a_r)
+    per = np.linalg.norm(a_g - a_r, axis=1) / np.linalg.norm(a_r, axis=1)
+    # per-body: the median body is far inside the bound
+    assert np.median(per) <= 1e-6, np.median(per)
+
+
+def test_rhs_mixed_masses_and_shift_invariance(gb, torch_cuda):
+    n = 2000
+    x = gb.ic_plummer(n, 5)
+    m = np.random.default_rng(2).uniform(0.5, 1.5, n)
+    m /= m.sum()
+    mt = gb.to_device(m)
+    ref = gb.nbody_rhs_f64(x, n, 0.01, masses=mt).cpu().numpy()
+    got = gb.nbody_rhs_mixed(x, n, 0.01, masses=mt).cpu().numpy()
+    assert _rel(got[3 * n:], ref[3 * n:]) <= 1e-6
+    # hi/lo positions relative to the centroid: a far-away system is as accurate
+    xs = x.copy()
+    xs[: 3 * n] += 1.0e4
+    got2 = gb.nbody_rhs_mixed(xs, n, 0.01, masses=mt).cpu().numpy()
+    assert _rel(got2[3 * n:], ref[3 * n:]) <= 2e-6
+
+
+def test_energy_kernel_matches_oracle(gb, orc, torch_cuda):
+    n = 777
+    x = gb.ic_plummer(n, 8)
+    ode, _ = orc.nbody_ode(n, 0.01, 1.0 / n)
+    e_ref = orc.energy(ode, x)
+    e = gb.energy(x, n, 0.01, 1.0 / n)
+    assert e["ke"] == pytest.approx(e_ref["ke"], rel=1e-13)
+    assert e["pe"] == pytest.approx(e_ref["pe"], rel=1e-12)
+    np.testing.assert_allclose(e["p"], e_ref["p"], atol=1e-14)
+    np.testing.assert_allclose(e["l"], e_ref["l"], atol=1e-13)
+
+
+def test_invalid_mixed_softening_rejected(gb, torch_cuda):
+    with pytest.raises(gb.GbError):
+        gb.nbody_rhs_mixed(_x(10, 1), 10, 0.0, 0.1)
