@@ -83,6 +83,8 @@ int gb_memcpy(void* dst, const void* src, size_t bytes, int32_t kind);
 int gb_memset_zero(void* ptr_dev, size_t bytes);
 int gb_fill_f64(double* ptr_dev, int64_t n, double value, gb_stream_t stream);
 int gb_stream_synchronize(gb_stream_t stream);
+/* Where a pointer lives: 0 host (pageable or pinned), 1 device, 2 managed. */
+int gb_pointer_kind(const void* ptr);
 
 /* ---------------------------------------------------------------------- */
 /* All-pairs softened gravity right-hand side (FP64).                      */

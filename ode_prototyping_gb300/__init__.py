@@ -103,6 +103,7 @@ SIGNATURES = {
     "gb_memset_zero": (C.c_int, [_VP, C.c_size_t]),
     "gb_fill_f64": (C.c_int, [_DP, _I64, _D, _VP]),
     "gb_stream_synchronize": (C.c_int, [_VP]),
+    "gb_pointer_kind": (C.c_int, [_VP]),
     "gb_nbody_rhs_f64": (C.c_int, [_DP, _DP, _I64, _D, _D, _DP, C.POINTER(GbForceTiling), _VP]),
     "gb_nbody_acc_f64": (C.c_int, [_DP, _DP, _I64, _D, _D, _DP, _I32, C.POINTER(GbForceTiling),
                                    _VP]),

@@ -151,6 +151,14 @@ __device__ __forceinline__ void force_f64_cta(const double* __restrict__ pos, lo
 // its running (sum, compensation) pair; the pair is widened to FP64 for the
 // lane and cluster combine.
 // ---------------------------------------------------------------------------
+// SFU reciprocal square root without the subnormal fix-up sequence: the
+// argument is r^2 + eps^2 >= eps^2 > 0, far from the subnormal range.
+__device__ __forceinline__ float rsqrt_sfu(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   const float y = __fsub_rn(v, c);
   const float t = __fadd_rn(s, y);
@@ -158,7 +166,7 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
-template <int T, int L, int BPT>
+template <int T, int L, int BPT, bool UNIFORM = false>
 __device__ __forceinline__ void force_mixed_cta(const PackedBody* __restrict__ packed, long long n,
                                                 long long i0, long long jb, long long je,
                                                 float eps2, PackedBody* sh, double (*part)[3]) {
@@ -205,8 +213,8 @@ __device__ __forceinline__ void force_mixed_cta(const PackedBody* __restrict__ p
         const float dy = (hw.y - hy[q]) + (lo.y - ly[q]);
         const float dz = (hw.z - hz[q]) + (lo.z - lz[q]);
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-        const float rinv = rsqrtf(r2);
-        const float s = (hw.w * rinv) * (rinv * rinv);
+        const float rinv = rsqrt_sfu(r2);
+        const float s = UNIFORM ? rinv * (rinv * rinv) : (hw.w * rinv) * (rinv * rinv);
         tx[q] = fmaf(s, dx, tx[q]);
         ty[q] = fmaf(s, dy, ty[q]);
         tz[q] = fmaf(s, dz, tz[q]);

@@ -185,8 +185,12 @@ __global__ void __launch_bounds__(T)
       force_f64_cta<T, L>(ysrc, n, i0, jb, je, P.eps2, P.masses, sh_pos, sh_m, part);
     } else {
       const PackedBody* src = (s == 0) ? P.PX + (long long)px * n : P.PY + (long long)(s & 1) * n;
-      force_mixed_cta<T, L, BPT>(src, n, i0, jb, je, P.eps2f,
-                                 reinterpret_cast<PackedBody*>(sh_raw), part);
+      if (P.masses)
+        force_mixed_cta<T, L, BPT, false>(src, n, i0, jb, je, P.eps2f,
+                                          reinterpret_cast<PackedBody*>(sh_raw), part);
+      else
+        force_mixed_cta<T, L, BPT, true>(src, n, i0, jb, je, P.eps2f,
+                                         reinterpret_cast<PackedBody*>(sh_raw), part);
     }
     cluster_combine<BI>(part, ci.rank, ci.size);
   }

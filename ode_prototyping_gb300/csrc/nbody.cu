@@ -94,7 +94,10 @@ __global__ void __launch_bounds__(T) rhs_mixed_kernel(const PackedBody* __restri
   const long long i0 = ci.itile * BI;
   long long jb, je;
   j_chunk(n, ci.rank, ci.size, T, jb, je);
-  force_mixed_cta<T, L, BPT>(packed, n, i0, jb, je, eps2, sh, part);
+  if (uniform_mass)
+    force_mixed_cta<T, L, BPT, true>(packed, n, i0, jb, je, eps2, sh, part);
+  else
+    force_mixed_cta<T, L, BPT, false>(packed, n, i0, jb, je, eps2, sh, part);
   cluster_combine<BI>(part, ci.rank, ci.size);
   if (ci.rank != 0) return;
   const long long nb = min((long long)BI, n - i0);

@@ -331,6 +331,20 @@ extern "C" int gb_fill_f64(double* p, int64_t n, double v, gb_stream_t stream) {
   return GB_OK;
 }
 
+extern "C" int gb_pointer_kind(const void* p) {
+  if (!p) return 0;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear: plain host memory
+    return 0;
+  }
+  switch (a.type) {
+    case cudaMemoryTypeDevice: return 1;
+    case cudaMemoryTypeManaged: return 2;
+    default: return 0;
+  }
+}
+
 extern "C" int gb_stream_synchronize(gb_stream_t stream) {
   GB_CUDA_TRY(cudaStreamSynchronize(as_cuda(stream)));
   return GB_OK;
