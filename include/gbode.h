@@ -326,6 +326,58 @@ int gb_integrate_nbody(const gb_tableau* tab, const gb_nbody_system* sys,
                        gb_integrate_stats* stats, gb_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
+/* Batched integrator: many independent N-body systems of uneven size,     */
+/* each following RKEmbeddedParallel<BT>::integrate's loop with its own    */
+/* step size, decision and status.  No counterpart in the reference (its   */
+/* state size is a compile-time constant, src/state/ODEState.hpp:7-23).    */
+/* Work units (system, i-tile) are ordered by cost and taken round-robin by */
+/* a persistent stage kernel; one warp per system runs its controller; an  */
+/* attempt is one CUDA graph replay.  Equal masses per system; scalar      */
+/* tolerances per system.  States are concatenated: system k occupies      */
+/* x[6*B_k .. 6*(B_k+N_k)) with B_k = N_0 + ... + N_{k-1}.                  */
+/* ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t threads_per_cta;   /* 64, 128, 256 (0 = 128) */
+  int32_t lanes;             /* lanes per body: 1, 2, 4 (0 = 2) */
+  int32_t bodies_per_thread; /* 1 or 2 (mixed precision; 0 = 1) */
+  int32_t grid_ctas;         /* persistent grid (0 = 8 CTAs per SM) */
+} gb_batch_tiling;
+
+typedef struct {
+  int32_t precision;         /* GB_PREC_* */
+  int32_t controller;        /* GB_CTRL_REFERENCE or GB_CTRL_PI */
+  int32_t fsal;
+  int32_t attempts_per_sync; /* attempts per graph replay (0 = 8) */
+  int64_t max_attempts;      /* per system, 0 = unlimited */
+  double host_wait_timeout_s;
+  double pi_beta;
+  gb_batch_tiling tiling;
+} gb_batch_opts;
+
+typedef struct gb_batch_s* gb_batch;
+
+int gb_batch_create(const gb_tableau* tab, int32_t n_systems, const int64_t* n_particles,
+                    const double* softening, const double* mass, const gb_batch_opts* opts,
+                    gb_stream_t stream, gb_batch* out);
+/* x0_dev: concatenated states; t0, tf, atol, rtol: host arrays, one per system. */
+int gb_batch_start(gb_batch b, const double* x0_dev, const double* t0, const double* tf,
+                   const double* atol, const double* rtol);
+/* Replays attempts until every system reaches its tf (or max_replays graph
+ * replays, 0 = no bound); returns the first failing system's status. */
+int gb_batch_advance(gb_batch b, int64_t max_replays);
+int gb_batch_enqueue(gb_batch b, int64_t n_replays);
+int gb_batch_sync(gb_batch b);
+/* totals: sums over systems (t = the smallest time); per_sys: n_systems entries or NULL. */
+int gb_batch_stats(gb_batch b, gb_integrate_stats* totals, gb_integrate_stats* per_sys);
+int gb_batch_state(gb_batch b, double* x_dev, double* t_host);
+int gb_batch_launch_stage(gb_batch b, int32_t stage);
+/* Times each candidate tile geometry and grid size on this batch and keeps
+ * the fastest (call after gb_batch_start). */
+int gb_batch_autotune(gb_batch b, int32_t reps, gb_batch_tiling* chosen, double* best_ms);
+int gb_batch_geometry(gb_batch b, gb_batch_tiling* out, int64_t* n_units);
+int gb_batch_destroy(gb_batch b);
+
+/* ---------------------------------------------------------------------- */
 /* Energy and momentum diagnostics (FP64).                                 */
 /* Replaces the softened potential and kinetic energies of                */
 /* scripts/nbody_physics/energy.py:146-192 (unit masses there), with       */

@@ -82,6 +82,18 @@ class GbMlp(C.Structure):
                 ("out_scale", C.c_float), ("out_bias", C.c_float)]
 
 
+class GbBatchTiling(C.Structure):
+    _fields_ = [("threads_per_cta", C.c_int32), ("lanes", C.c_int32),
+                ("bodies_per_thread", C.c_int32), ("grid_ctas", C.c_int32)]
+
+
+class GbBatchOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("controller", C.c_int32), ("fsal", C.c_int32),
+                ("attempts_per_sync", C.c_int32), ("max_attempts", C.c_int64),
+                ("host_wait_timeout_s", C.c_double), ("pi_beta", C.c_double),
+                ("tiling", GbBatchTiling)]
+
+
 class GbStepLog(C.Structure):
     _fields_ = [("feat", C.c_float * MLP_IN), ("log_dt", C.c_float), ("log_err", C.c_float),
                 ("accepted", C.c_float), ("log_dt_ideal", C.c_float)]
@@ -143,6 +155,20 @@ SIGNATURES = {
     "gb_integrate_nbody": (C.c_int, [C.POINTER(GbTableau), C.POINTER(GbNBodySystem),
                                      C.POINTER(GbIntegrateOpts), _DP, _D, _D, _DP, _DP, _D, _D,
                                      SAVE_FN, _VP, _DP, C.POINTER(GbIntegrateStats), _VP]),
+    "gb_batch_create": (C.c_int, [C.POINTER(GbTableau), _I32, C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(GbBatchOpts), _VP, C.POINTER(C.c_void_p)]),
+    "gb_batch_start": (C.c_int, [_VP, _DP, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "gb_batch_advance": (C.c_int, [_VP, _I64]),
+    "gb_batch_enqueue": (C.c_int, [_VP, _I64]),
+    "gb_batch_sync": (C.c_int, [_VP]),
+    "gb_batch_stats": (C.c_int, [_VP, C.POINTER(GbIntegrateStats), C.POINTER(GbIntegrateStats)]),
+    "gb_batch_state": (C.c_int, [_VP, _DP, C.POINTER(C.c_double)]),
+    "gb_batch_launch_stage": (C.c_int, [_VP, _I32]),
+    "gb_batch_autotune": (C.c_int, [_VP, _I32, C.POINTER(GbBatchTiling), C.POINTER(C.c_double)]),
+    "gb_batch_geometry": (C.c_int, [_VP, C.POINTER(GbBatchTiling), C.POINTER(C.c_int64)]),
+    "gb_batch_destroy": (C.c_int, [_VP]),
     "gb_nbody_energy_workspace_bytes": (C.c_size_t, [_I64]),
     "gb_nbody_energy_f64": (C.c_int, [_DP, _I64, _D, _D, _DP, _VP, C.c_size_t, _DP, _VP]),
     "gb_ic_uniform_ball": (C.c_int, [_I64, C.c_uint64, _D, C.POINTER(C.c_double)]),
@@ -554,6 +580,108 @@ class RKEmbeddedParallel:
             return st
         finally:
             it.close()
+
+
+def _dbl(values):
+    arr = np.ascontiguousarray(values, dtype=np.float64)
+    return arr, arr.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Batch:
+    """Many independent N-body systems advanced together (gb_batch_*)."""
+
+    def __init__(self, tab, n_particles, softening, mass=None, precision="f64",
+                 controller="reference", attempts_per_sync=8, fsal=True, max_attempts=0,
+                 tiling: GbBatchTiling | None = None, stream=None):
+        self.tab = tableau(tab)
+        self.n = np.ascontiguousarray(n_particles, dtype=np.int64)
+        self.ns = len(self.n)
+        self.offsets = np.concatenate([[0], np.cumsum(self.n)]) * 6
+        self._soft, sp = _dbl(np.broadcast_to(softening, (self.ns,)))
+        m = 1.0 / self.n if mass is None else np.broadcast_to(mass, (self.ns,))
+        self._mass, mp = _dbl(m)
+        o = GbBatchOpts()
+        o.precision = PREC[precision]
+        o.controller = CONTROLLERS[controller]
+        o.fsal = 1 if fsal else 0
+        o.attempts_per_sync = attempts_per_sync
+        o.max_attempts = max_attempts
+        o.host_wait_timeout_s = 600.0
+        if tiling is not None:
+            o.tiling = tiling
+        self.opts = o
+        h = C.c_void_p()
+        check(lib().gb_batch_create(C.byref(self.tab), self.ns,
+                                    self.n.ctypes.data_as(C.POINTER(C.c_int64)), sp, mp,
+                                    C.byref(o), _stream(stream), C.byref(h)), "gb_batch_create")
+        self.h = h
+
+    def start(self, x0_concat, t0, tf, atol, rtol):
+        x0 = to_device(x0_concat)
+        self._x0 = x0
+        a = [_dbl(np.broadcast_to(v, (self.ns,))) for v in (t0, tf, atol, rtol)]
+        self._keep = a
+        check(lib().gb_batch_start(self.h, _ptr(x0), *(p for _, p in a)), "gb_batch_start")
+
+    def advance(self, max_replays: int = 0) -> int:
+        return lib().gb_batch_advance(self.h, max_replays)
+
+    def enqueue(self, n: int):
+        check(lib().gb_batch_enqueue(self.h, n), "gb_batch_enqueue")
+
+    def sync(self):
+        check(lib().gb_batch_sync(self.h), "gb_batch_sync")
+
+    def stats(self, per_system: bool = False):
+        tot = GbIntegrateStats()
+        per = (GbIntegrateStats * self.ns)() if per_system else None
+        check(lib().gb_batch_stats(self.h, C.byref(tot), per), "gb_batch_stats")
+        d = {f: getattr(tot, f) for f, _ in GbIntegrateStats._fields_}
+        if per_system:
+            d["systems"] = [{f: getattr(p, f) for f, _ in GbIntegrateStats._fields_}
+                            for p in per]
+        return d
+
+    def state(self):
+        torch = _torch()
+        out = torch.empty(int(self.offsets[-1]), dtype=torch.float64, device="cuda")
+        t = np.zeros(self.ns)
+        check(lib().gb_batch_state(self.h, _ptr(out), t.ctypes.data_as(C.POINTER(C.c_double))),
+              "gb_batch_state")
+        return out, t
+
+    def system_state(self, x, k):
+        return x[self.offsets[k]:self.offsets[k + 1]]
+
+    def launch_stage(self, s: int):
+        check(lib().gb_batch_launch_stage(self.h, s), "gb_batch_launch_stage")
+
+    def autotune(self, reps: int = 3) -> dict:
+        t = GbBatchTiling()
+        ms = C.c_double(0)
+        check(lib().gb_batch_autotune(self.h, reps, C.byref(t), C.byref(ms)), "gb_batch_autotune")
+        return {"threads_per_cta": t.threads_per_cta, "lanes": t.lanes,
+                "bodies_per_thread": t.bodies_per_thread, "grid_ctas": t.grid_ctas,
+                "stage_ms": ms.value}
+
+    def geometry(self) -> dict:
+        t = GbBatchTiling()
+        nu = C.c_int64(0)
+        check(lib().gb_batch_geometry(self.h, C.byref(t), C.byref(nu)), "gb_batch_geometry")
+        return {"threads_per_cta": t.threads_per_cta, "lanes": t.lanes,
+                "bodies_per_thread": t.bodies_per_thread, "grid_ctas": t.grid_ctas,
+                "units": int(nu.value)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def exported_symbols() -> list[str]:

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "integrator.cuh"
+#include "mlp.cuh"
 
 namespace gb {
 
@@ -45,6 +46,106 @@ __device__ __forceinline__ double pi_step(Ctrl& c, double dt, double err, bool a
   double dtn = dt * scale;
   if (dtn / (c.tf - c.t0) < 1.0e-12) dtn = (c.tf - c.t0) * 1.0e-12;
   return dtn;
+}
+
+// Per-system environment of the end-of-attempt decision.
+struct CtrlEnv {
+  StepLog* log;          // controller log (training data) or null
+  long long log_capacity;
+  double* times_ring;    // time of each ring slot, or null
+  int R;                 // ring slots
+  long long n;           // bodies
+};
+
+// Shifts the step/error history as finish_attempt will (used to build the
+// learned controller's features before the decision is applied).
+__device__ __forceinline__ void preview_history(Ctrl& c, double err, bool accepted) {
+  for (int k = 2; k > 0; --k) {
+    c.dt_hist[k] = c.dt_hist[k - 1];
+    c.err_hist[k] = c.err_hist[k - 1];
+  }
+  c.dt_hist[0] = c.dt;
+  c.err_hist[0] = isfinite(err) ? err : 1e300;
+  c.last_accepted = accepted ? 1 : 0;
+}
+
+// End-of-attempt decision by one thread: acceptance (err <= 1,
+// RKEmbeddedParallel.hpp:58-62), step-size update (:65-74 or PI or learned),
+// last-step clamp (:77-79) and the loop condition t < tf (:35).
+__device__ inline void finish_attempt(const DevTableau& tab, const CtrlEnv& P, Ctrl& c,
+                                      double err, double learned_log_scale, bool have_learned) {
+  const double dt = c.dt;
+  c.err = err;
+  c.n_attempts += 1;
+  const bool finite = isfinite(err);
+  const bool accepted = finite && err <= 1.0;
+  if (c.learned_active) {
+    c.n_learned += 1;
+    if (!accepted) c.n_learned_rejected += 1;
+  }
+  preview_history(c, err, accepted);
+  // controller log (training data of the learned controller): the features
+  // the controller sees after this attempt, and the attempt's outcome
+  if (P.log && c.log_count < P.log_capacity) {
+    StepLog& L = P.log[c.log_count];
+    make_features(c, tab, P.n, L.feat);
+    L.log_dt = (float)log(dt);
+    L.log_err = (float)log(fmax(err, 1e-300));
+    L.accepted = accepted ? 1.f : 0.f;
+    double ideal = finite ? dt * c.safety / pow(fmax(err, 1e-300), 1.0 / (1.0 + c.q)) : dt * 0.33;
+    L.log_dt_ideal = (float)log(ideal);
+    c.log_count += 1;
+  }
+  if (!finite) {
+    c.status = GB_ERR_NOT_FINITE;
+    c.done = 1;
+    return;
+  }
+  if (accepted) {
+    c.t += dt;
+    c.cur = (c.cur + 1) % P.R;
+    if (P.times_ring) P.times_ring[c.cur] = c.t;
+    c.n_accepted += 1;
+    c.px ^= 1;
+    if (c.fsal) {
+      c.k0slot = (c.k0slot == 0) ? tab.n_stages - 1 : 0;
+      c.k0_valid = 1;
+    } else {
+      c.k0_valid = 0;
+    }
+  } else {
+    c.n_rejected += 1;
+    c.k0_valid = 1;  // x0 unchanged: f(x0) is still in its slot
+  }
+  double dtn;
+  c.learned_active = 0;
+  if (c.controller == GB_CTRL_PI) {
+    dtn = pi_step(c, dt, err, accepted);
+  } else if (c.controller == GB_CTRL_LEARNED) {
+    if (accepted && have_learned) {
+      // The network proposes the next step; the embedded error estimate of
+      // that attempt still decides acceptance.
+      double scale = exp(fmin(fmax(learned_log_scale, -1.1), 1.79));  // within [0.33, 6.0]
+      if (c.reject_prev) scale = fmin(scale, 1.0);
+      dtn = dt * scale;
+      c.learned_dt = dtn;
+      c.learned_active = 1;
+      // keep the PI memory current
+      c.err_prev = fmax(err, 1.0e-4);
+      c.reject_prev = 0;
+    } else {
+      dtn = pi_step(c, dt, err, accepted);  // fallback on every rejection
+    }
+  } else {
+    dtn = reference_step(dt, err, c.safety, c.q, c.t0, c.tf);
+  }
+  c.dt = dtn;
+  if (c.t + c.dt > c.tf) c.dt = c.tf - c.t;
+  if (!(c.t < c.tf)) c.done = 1;
+  if (!c.done && c.max_attempts > 0 && c.n_attempts >= c.max_attempts) {
+    c.status = GB_ERR_BUDGET;
+    c.done = 1;
+  }
 }
 
 }  // namespace gb

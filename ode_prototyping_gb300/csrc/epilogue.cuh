@@ -1,0 +1,151 @@
+// epilogue.cuh -- row-local work that follows the accelerations of one stage:
+// the stage derivative k_s = (v, a), then either the next stage state
+//   y_{s+1} = x0 + dt * sum_{l<=s} a[s][l] k_l       (rk_stage_kernel,
+//   RKEmbeddedParallel.hpp:91-101), or, after the last stage,
+//   x = x0 + dt * sum b_l k_l,  err = dt * sum (b_l - bt_l) k_l   (:103-123),
+//   target = atol + rtol * max(|x|, |x0|)                          (:125-130),
+//   (err / target)^2                                              (:132-137),
+// each in the reference's accumulation order with IEEE operations.  Used by
+// the single-system fused kernel and by the batched kernel.
+#pragma once
+
+#include "integrator.cuh"
+
+namespace gb {
+
+__device__ __forceinline__ int kslot(int l, int S, int k0slot) {
+  if (l == 0) return k0slot;
+  if (l == S - 1) return k0slot == 0 ? S - 1 : 0;
+  return l;
+}
+
+struct EpiCtx {
+  const DevTableau* tab;
+  int s, S, k0slot;
+  bool skip_force, last, exact;
+  double dt;
+  long long n;           // bodies of the system
+  const double* x0;      // all pointers below are already offset to the system
+  const double* ysrc;    // stage state whose velocities give dx/dt
+  double* ks;            // stage slot l is ks + l * kstride
+  long long kstride;
+  double* ynext;         // y_{s+1}
+  double* xnew;          // candidate state (last stage)
+  PackedBody* pnext;     // packed positions of y_{s+1} or x (mixed path)
+  const double* atol;    // per-element tolerances or null (scalars below)
+  const double* rtol;
+  double atol_s, rtol_s;
+  const double* masses;  // per-body masses or null (uniform `mass`)
+  double mass;
+  const double* cref;    // hi/lo reference point
+  double* sq;            // per-element squares (exact mode) or null
+};
+
+// One body's six state elements.  `acc` is the unscaled pair sum (ignored
+// when the stage derivative is reused).  Adds the body's scaled squares to
+// sq_acc (last stage) and its |a| to amax (stage 0).
+template <int PREC>
+__device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, const double* acc,
+                                              double& sq_acc, double& amax) {
+  const DevTableau& tab = *E.tab;
+  const int s = E.s, S = E.S;
+  const long long n = E.n;
+  long long idx[6];
+  double k[6];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    idx[c] = 3 * i + c;
+    idx[3 + c] = 3 * n + 3 * i + c;
+  }
+  double* ks_s = E.ks + (long long)kslot(s, S, E.k0slot) * E.kstride;
+  if (E.skip_force) {
+#pragma unroll
+    for (int e = 0; e < 6; ++e) k[e] = ks_s[idx[e]];
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      k[c] = E.ysrc[idx[3 + c]];  // dx/dt = v (nbody_init_dxdt_kernel)
+      k[3 + c] = E.masses ? acc[c] : dmul(acc[c], E.mass);
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) ks_s[idx[e]] = k[e];
+    if (s == 0) amax = fmax(amax, sqrt(k[3] * k[3] + k[4] * k[4] + k[5] * k[5]));
+  }
+  if (!E.last) {
+    double yn[6];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      double v = 0.0;
+      for (int l = 0; l <= s; ++l) {
+        const double a = tab.a[s][l];
+        if (a == 0.0) continue;
+        const double kl = (l == s) ? k[e] : E.ks[(long long)kslot(l, S, E.k0slot) * E.kstride + idx[e]];
+        v = dadd(v, dmul(a, kl));
+      }
+      yn[e] = dadd(E.x0[idx[e]], dmul(v, E.dt));
+      E.ynext[idx[e]] = yn[e];
+    }
+    if constexpr (PREC == GB_PREC_MIXED) {
+      const float w = E.masses ? (float)E.masses[i] : 1.0f;
+      E.pnext[i] = pack_body(yn[0], yn[1], yn[2], E.cref[0], E.cref[1], E.cref[2], w);
+    }
+  } else {
+    double xn[6];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      double xv = 0.0, ev = 0.0;
+      for (int l = 0; l < S; ++l) {
+        const double bb = tab.b[l], db = tab.db[l];
+        if (bb == 0.0 && db == 0.0) continue;
+        const double kl = (l == s) ? k[e] : E.ks[(long long)kslot(l, S, E.k0slot) * E.kstride + idx[e]];
+        if (bb != 0.0) xv = dadd(xv, dmul(bb, kl));
+        if (db != 0.0) ev = dadd(ev, dmul(db, kl));
+      }
+      const double x0e = E.x0[idx[e]];
+      xn[e] = dadd(x0e, dmul(xv, E.dt));
+      const double er = dmul(ev, E.dt);
+      E.xnew[idx[e]] = xn[e];
+      const double at = E.atol ? E.atol[idx[e]] : E.atol_s;
+      const double rt = E.rtol ? E.rtol[idx[e]] : E.rtol_s;
+      const double ax = fabs(xn[e]), ax0 = fabs(x0e);
+      const double tg = dadd(at, dmul(rt, ax < ax0 ? ax0 : ax));
+      const double q = __ddiv_rn(er, tg);
+      const double sq = dmul(q, q);
+      if (E.exact) {
+        E.sq[idx[e]] = sq;
+      } else {
+        sq_acc = dadd(sq_acc, sq);
+      }
+    }
+    if constexpr (PREC == GB_PREC_MIXED) {
+      const float w = E.masses ? (float)E.masses[i] : 1.0f;
+      E.pnext[i] = pack_body(xn[0], xn[1], xn[2], E.cref[0], E.cref[1], E.cref[2], w);
+    }
+  }
+}
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = dadd(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+}  // namespace gb

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "controller.cuh"
+#include "epilogue.cuh"
 #include "mlp.cuh"
 
 namespace gb {
@@ -31,127 +32,6 @@ int launch_norm(const double* v, const double* s, long long n, double* partial, 
 size_t norm_workspace_bytes(long long n);
 
 namespace {
-
-__device__ __forceinline__ int kslot(int l, int S, int k0slot) {
-  if (l == 0) return k0slot;
-  if (l == S - 1) return k0slot == 0 ? S - 1 : 0;
-  return l;
-}
-
-__device__ __forceinline__ double block_sum(double v, double* red) {
-  red[threadIdx.x] = v;
-  __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st /= 2) {
-    if ((int)threadIdx.x < st) red[threadIdx.x] = dadd(red[threadIdx.x], red[threadIdx.x + st]);
-    __syncthreads();
-  }
-  double r = red[0];
-  __syncthreads();
-  return r;
-}
-
-__device__ __forceinline__ double block_max(double v, double* red) {
-  red[threadIdx.x] = v;
-  __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st /= 2) {
-    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
-    __syncthreads();
-  }
-  double r = red[0];
-  __syncthreads();
-  return r;
-}
-
-// End-of-attempt decision by one thread: acceptance (err <= 1,
-// RKEmbeddedParallel.hpp:58-62), step-size update (:65-74 or PI or learned),
-// last-step clamp (:77-79) and the loop condition t < tf (:35).
-// Shifts the step/error history as finish_attempt will (used to build the
-// learned controller's features before the decision is applied).
-__device__ __forceinline__ void preview_history(Ctrl& c, double err, bool accepted) {
-  for (int k = 2; k > 0; --k) {
-    c.dt_hist[k] = c.dt_hist[k - 1];
-    c.err_hist[k] = c.err_hist[k - 1];
-  }
-  c.dt_hist[0] = c.dt;
-  c.err_hist[0] = isfinite(err) ? err : 1e300;
-  c.last_accepted = accepted ? 1 : 0;
-}
-
-__device__ void finish_attempt(const DevTableau& tab, const FusedParams& P, Ctrl& c, double err,
-                               double learned_log_scale, bool have_learned) {
-  const double dt = c.dt;
-  c.err = err;
-  c.n_attempts += 1;
-  const bool finite = isfinite(err);
-  const bool accepted = finite && err <= 1.0;
-  if (c.learned_active) {
-    c.n_learned += 1;
-    if (!accepted) c.n_learned_rejected += 1;
-  }
-  preview_history(c, err, accepted);
-  // controller log (training data of the learned controller): the features
-  // the controller sees after this attempt, and the attempt's outcome
-  if (P.log && c.log_count < P.log_capacity) {
-    StepLog& L = P.log[c.log_count];
-    make_features(c, tab, P.n, L.feat);
-    L.log_dt = (float)log(dt);
-    L.log_err = (float)log(fmax(err, 1e-300));
-    L.accepted = accepted ? 1.f : 0.f;
-    double ideal = finite ? dt * c.safety / pow(fmax(err, 1e-300), 1.0 / (1.0 + c.q)) : dt * 0.33;
-    L.log_dt_ideal = (float)log(ideal);
-    c.log_count += 1;
-  }
-  if (!finite) {
-    c.status = GB_ERR_NOT_FINITE;
-    c.done = 1;
-    return;
-  }
-  if (accepted) {
-    c.t += dt;
-    c.cur = (c.cur + 1) % P.R;
-    P.times_ring[c.cur] = c.t;
-    c.n_accepted += 1;
-    c.px ^= 1;
-    if (c.fsal) {
-      c.k0slot = (c.k0slot == 0) ? tab.n_stages - 1 : 0;
-      c.k0_valid = 1;
-    } else {
-      c.k0_valid = 0;
-    }
-  } else {
-    c.n_rejected += 1;
-    c.k0_valid = 1;  // x0 unchanged: f(x0) is still in its slot
-  }
-  double dtn;
-  c.learned_active = 0;
-  if (c.controller == GB_CTRL_PI) {
-    dtn = pi_step(c, dt, err, accepted);
-  } else if (c.controller == GB_CTRL_LEARNED) {
-    if (accepted && have_learned) {
-      // The network proposes the next step; the embedded error estimate of
-      // that attempt still decides acceptance.
-      double scale = exp(fmin(fmax(learned_log_scale, -1.1), 1.79));  // within [0.33, 6.0]
-      if (c.reject_prev) scale = fmin(scale, 1.0);
-      dtn = dt * scale;
-      c.learned_dt = dtn;
-      c.learned_active = 1;
-      // keep the PI memory current
-      c.err_prev = fmax(err, 1.0e-4);
-      c.reject_prev = 0;
-    } else {
-      dtn = pi_step(c, dt, err, accepted);  // fallback on every rejection
-    }
-  } else {
-    dtn = reference_step(dt, err, c.safety, c.q, c.t0, c.tf);
-  }
-  c.dt = dtn;
-  if (c.t + c.dt > c.tf) c.dt = c.tf - c.t;
-  if (!(c.t < c.tf)) c.done = 1;
-  if (!c.done && c.max_attempts > 0 && c.n_attempts >= c.max_attempts) {
-    c.status = GB_ERR_BUDGET;
-    c.done = 1;
-  }
-}
 
 template <int PREC, int T, int L, int BPT>
 __global__ void __launch_bounds__(T)
@@ -197,89 +77,35 @@ __global__ void __launch_bounds__(T)
   if (ci.rank != 0) return;
 
   const long long nb = min((long long)BI, n - i0);
-  double* ks_s = P.ks + (long long)kslot(s, S, k0slot) * n_var;
   const bool last = (s == S - 1);
+  EpiCtx E;
+  E.tab = &tab;
+  E.s = s;
+  E.S = S;
+  E.k0slot = k0slot;
+  E.skip_force = skip_force;
+  E.last = last;
+  E.exact = P.exact != 0;
+  E.dt = dt;
+  E.n = n;
+  E.x0 = x0;
+  E.ysrc = ysrc;
+  E.ks = P.ks;
+  E.kstride = n_var;
+  E.ynext = P.Y + (long long)((s + 1) & 1) * n_var;
+  E.xnew = P.ring + (long long)((cur + 1) % P.R) * n_var;
+  E.pnext = last ? P.PX + (long long)(px ^ 1) * n : P.PY + (long long)((s + 1) & 1) * n;
+  E.atol = P.atol;
+  E.rtol = P.rtol;
+  E.atol_s = P.atol_s;
+  E.rtol_s = P.rtol_s;
+  E.masses = P.masses;
+  E.mass = P.mass;
+  E.cref = P.cref;
+  E.sq = P.sq;
   double sq_acc = 0.0;
   double amax = 0.0;
-  for (int b = threadIdx.x; b < nb; b += T) {
-    const long long i = i0 + b;
-    long long idx[6];
-    double k[6];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      idx[c] = 3 * i + c;
-      idx[3 + c] = 3 * n + 3 * i + c;
-    }
-    if (skip_force) {
-#pragma unroll
-      for (int e = 0; e < 6; ++e) k[e] = ks_s[idx[e]];
-    } else {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        k[c] = ysrc[idx[3 + c]];  // dx/dt = v (nbody_init_dxdt_kernel)
-        double a = part[b][c];
-        if (!P.masses) a = dmul(a, P.mass);
-        k[3 + c] = a;
-      }
-#pragma unroll
-      for (int e = 0; e < 6; ++e) ks_s[idx[e]] = k[e];
-      if (s == 0) amax = fmax(amax, sqrt(k[3] * k[3] + k[4] * k[4] + k[5] * k[5]));
-    }
-    if (!last) {
-      double yn[6];
-#pragma unroll
-      for (int e = 0; e < 6; ++e) {
-        double v = 0.0;
-        for (int l = 0; l <= s; ++l) {
-          const double a = tab.a[s][l];
-          if (a == 0.0) continue;
-          const double kl = (l == s) ? k[e] : P.ks[(long long)kslot(l, S, k0slot) * n_var + idx[e]];
-          v = dadd(v, dmul(a, kl));
-        }
-        yn[e] = dadd(x0[idx[e]], dmul(v, dt));
-        P.Y[(long long)((s + 1) & 1) * n_var + idx[e]] = yn[e];
-      }
-      if constexpr (PREC == GB_PREC_MIXED) {
-        const float w = P.masses ? (float)P.masses[i] : 1.0f;
-        P.PY[(long long)((s + 1) & 1) * n + i] =
-            pack_body(yn[0], yn[1], yn[2], P.cref[0], P.cref[1], P.cref[2], w);
-      }
-    } else {
-      double xn[6];
-      double* xnew = P.ring + (long long)((cur + 1) % P.R) * n_var;
-#pragma unroll
-      for (int e = 0; e < 6; ++e) {
-        double xv = 0.0, ev = 0.0;
-        for (int l = 0; l < S; ++l) {
-          const double bb = tab.b[l], db = tab.db[l];
-          if (bb == 0.0 && db == 0.0) continue;
-          const double kl = (l == s) ? k[e] : P.ks[(long long)kslot(l, S, k0slot) * n_var + idx[e]];
-          if (bb != 0.0) xv = dadd(xv, dmul(bb, kl));
-          if (db != 0.0) ev = dadd(ev, dmul(db, kl));
-        }
-        const double x0e = x0[idx[e]];
-        xn[e] = dadd(x0e, dmul(xv, dt));
-        const double er = dmul(ev, dt);
-        xnew[idx[e]] = xn[e];
-        const double at = P.atol ? P.atol[idx[e]] : P.atol_s;
-        const double rt = P.rtol ? P.rtol[idx[e]] : P.rtol_s;
-        const double ax = fabs(xn[e]), ax0 = fabs(x0e);
-        const double tg = dadd(at, dmul(rt, ax < ax0 ? ax0 : ax));
-        const double q = __ddiv_rn(er, tg);
-        const double sq = dmul(q, q);
-        if (P.exact) {
-          P.sq[idx[e]] = sq;
-        } else {
-          sq_acc = dadd(sq_acc, sq);
-        }
-      }
-      if constexpr (PREC == GB_PREC_MIXED) {
-        const float w = P.masses ? (float)P.masses[i] : 1.0f;
-        P.PX[(long long)(px ^ 1) * n + i] =
-            pack_body(xn[0], xn[1], xn[2], P.cref[0], P.cref[1], P.cref[2], w);
-      }
-    }
-  }
+  for (int b = threadIdx.x; b < nb; b += T) body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
   if (s == 0 && !skip_force) {
     const double m = block_max(amax, red);
     if (threadIdx.x == 0) P.aux[ci.itile] = m;
@@ -352,7 +178,8 @@ __global__ void __launch_bounds__(256)
     if (!k0_valid) c.max_abs_acc = amax_all;
     c.n_rhs += k0_valid ? S - 1 : S;
     if (k0_valid) c.n_rhs_saved += 1;
-    finish_attempt(tab, P, c, err, sh_flag ? (double)outv : 0.0, sh_flag != 0);
+    const CtrlEnv env{P.log, P.log_capacity, P.times_ring, P.R, P.n};
+    finish_attempt(tab, env, c, err, sh_flag ? (double)outv : 0.0, sh_flag != 0);
     *C = c;
   }
 }

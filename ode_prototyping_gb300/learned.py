@@ -1,0 +1,142 @@
+"""Learned step-size proposer: data, training and evaluation.
+
+1. ``collect_logs`` runs the plain integrator with the device-side controller
+   log on (``log_steps``): per attempt, the 16 features the controller sees
+   after the attempt, the attempted step, the scaled error and the decision.
+2. ``build_dataset`` pairs every accepted attempt k with the next attempt
+   k+1 and sets the target to the step change that would have put attempt
+   k+1 at the error ratio rho under the local error model err ~ dt^(q+1):
+   r_k = log(dt_{k+1} (rho / err_{k+1})^(1/(q+1))) - log(dt_k).
+3. ``train`` fits the 16 -> 64 -> 64 -> 1 SiLU network with the library's
+   own forward / backward / Adam kernels (``gb_mlp_train``), asymmetric loss
+   (over-long steps cost a rejected attempt, so over-prediction weighs more).
+4. ``evaluate`` integrates held-out systems with the reference, PI and
+   learned controllers and reports RHS evaluations, rejected fraction,
+   accepted steps per second and the relative energy error.
+
+The embedded error estimate still accepts or rejects every attempt, and
+every rejection hands the step back to the PI controller.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import (GbMlp, GbIntegrateStats, Gb300Executor, Integrator, NBodyODE, check, energy,
+               ic_plummer, lib, tableau)
+
+FEAT, LOG_DT, LOG_ERR, ACCEPTED = slice(0, 16), 16, 17, 18
+
+
+def collect_logs(seeds, n: int, softening: float, tab: str, tol: float, tf: float,
+                 attempts: int, precision: str = "mixed", controller: str = "reference"):
+    logs = []
+    for seed in seeds:
+        x0 = ic_plummer(n, seed)
+        exe = Gb300Executor(precision=precision, controller=controller, attempts_per_sync=16,
+                            log_steps=attempts)
+        it = Integrator(tab, NBodyODE(n, softening, 1.0 / n), exe)
+        it.start(x0, 0.0, tf, tol, tol)
+        it.advance(attempts)
+        logs.append(it.log())
+        it.close()
+    return logs
+
+
+def build_dataset(logs, q: int, rho: float = 0.5):
+    xs, ys = [], []
+    for rec in logs:
+        for k in range(len(rec) - 1):
+            if rec[k, ACCEPTED] < 0.5:
+                continue
+            target = (rec[k + 1, LOG_DT] + (np.log(rho) - rec[k + 1, LOG_ERR]) / (q + 1)
+                      - rec[k, LOG_DT])
+            if not np.isfinite(target):
+                continue
+            xs.append(rec[k, FEAT])
+            ys.append(target)
+    return np.asarray(xs, dtype=np.float32), np.asarray(ys, dtype=np.float32)
+
+
+def _to_device_struct(m: GbMlp):
+    import torch
+    buf = torch.empty(C.sizeof(GbMlp), dtype=torch.uint8, device="cuda")
+    host = torch.frombuffer(bytearray(bytes(m)), dtype=torch.uint8)
+    buf.copy_(host)
+    return buf
+
+
+def _from_device_struct(buf) -> GbMlp:
+    raw = bytes(buf.cpu().numpy().tobytes())
+    return GbMlp.from_buffer_copy(raw)
+
+
+def train(x: np.ndarray, y: np.ndarray, epochs: int = 3000, lr: float = 3e-3,
+          over_weight: float = 3.0, seed: int = 0):
+    """Returns (trained gb_mlp in host memory, final loss)."""
+    import torch
+    m = GbMlp()
+    check(lib().gb_mlp_init(C.byref(m), seed), "gb_mlp_init")
+    mean = x.mean(0)
+    std = x.std(0)
+    scale = np.where(std > 1e-6, 1.0 / np.maximum(std, 1e-6), 0.0)
+    for k in range(16):
+        m.in_mean[k] = float(mean[k])
+        m.in_scale[k] = float(scale[k])
+    m.out_bias = float(y.mean())
+    m.out_scale = float(max(y.std(), 1e-3))
+    w = _to_device_struct(m)
+    xd = torch.as_tensor(np.ascontiguousarray(x), device="cuda")
+    yd = torch.as_tensor(np.ascontiguousarray(y), device="cuda")
+    loss = C.c_float(0)
+    check(lib().gb_mlp_train(w.data_ptr(), xd.data_ptr(), yd.data_ptr(), len(y), epochs, lr,
+                             over_weight, C.byref(loss), None), "gb_mlp_train")
+    torch.cuda.synchronize()
+    return _from_device_struct(w), float(loss.value)
+
+
+def run_window(n: int, softening: float, tab: str, tol: float, t_end: float, seed: int,
+               controller: str, mlp: GbMlp | None = None, precision: str = "mixed") -> dict:
+    import torch
+    x0 = ic_plummer(n, seed)
+    stream = torch.cuda.Stream()
+    exe = Gb300Executor(precision=precision, controller=controller, attempts_per_sync=16,
+                        mlp=mlp)
+    it = Integrator(tab, NBodyODE(n, softening, 1.0 / n), exe, stream=stream)
+    e0 = energy(x0, n, softening, 1.0 / n)
+    it.start(x0, 0.0, t_end, tol, tol)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = it.advance(0)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    st = it.stats()
+    xs, t = it.state()
+    e1 = energy(xs, n, softening, 1.0 / n)
+    it.close()
+    return {"controller": controller, "status": rc, "t": t, "wall_s": wall,
+            "accepted": st["n_accepted"], "rejected": st["n_rejected"],
+            "attempts": st["n_attempts"], "rhs": st["n_rhs"],
+            "rejected_fraction": st["n_rejected"] / max(st["n_attempts"], 1),
+            "accepted_steps_per_s": st["n_accepted"] / wall,
+            "learned_proposals": st["n_learned_proposals"],
+            "learned_rejected": st["n_learned_rejected"],
+            "energy_rel_err": abs(e1["e"] - e0["e"]) / abs(e0["e"]), "state": xs}
+
+
+def evaluate(n, softening, tab, tol, t_end, seeds, mlp, precision="mixed"):
+    out = {}
+    for ctl in ("reference", "pi", "learned"):
+        rows = [run_window(n, softening, tab, tol, t_end, s, ctl,
+                           mlp if ctl == "learned" else None, precision) for s in seeds]
+        agg = {k: float(np.sum([r[k] for r in rows])) for k in
+               ("wall_s", "accepted", "rejected", "attempts", "rhs", "learned_proposals",
+                "learned_rejected")}
+        agg["rejected_fraction"] = agg["rejected"] / max(agg["attempts"], 1)
+        agg["energy_rel_err_max"] = float(max(r["energy_rel_err"] for r in rows))
+        agg["simulated_time_per_s"] = len(seeds) * t_end / agg["wall_s"]
+        agg["states"] = [r["state"] for r in rows]
+        out[ctl] = agg
+    return out

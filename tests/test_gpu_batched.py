@@ -1,0 +1,65 @@
+"""GPU: the batched integrator -- every system of a batch of uneven sizes
+follows the reference's loop (oracle) and agrees with the single-system
+integrator."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _systems(gb, sizes, seed0):
+    xs = [gb.ic_plummer(int(n), seed0 + k) for k, n in enumerate(sizes)]
+    return xs, np.concatenate(xs)
+
+
+@pytest.mark.parametrize("tab", ["DOPRI5", "RKF78"])
+def test_batch_f64_matches_oracle_per_system(gb, orc, torch_cuda, tab):
+    sizes = [33, 64, 100, 129, 7, 250]
+    soft, tol, tf = 0.05, 1e-9, 0.15
+    xs, x0 = _systems(gb, sizes, 40)
+    b = gb.Batch(tab, sizes, soft, precision="f64")
+    b.start(x0, 0.0, tf, tol, tol)
+    assert b.advance() == 0
+    st = b.stats(per_system=True)
+    x, t = b.state()
+    x = x.cpu().numpy()
+    for k, n in enumerate(sizes):
+        ode, _ = orc.nbody_ode(n, soft, 1.0 / n)
+        r = orc.integrate(tab, ode, xs[k], 0.0, tf, tol, tol)
+        assert st["systems"][k]["n_accepted"] == len(r.times) - 1, k
+        assert t[k] == r.times[-1]
+        assert np.max(np.abs(b.system_state(x, k) - r.states[-1])) <= 10 * tol
+    b.close()
+
+
+def test_batch_mixed_and_autotune(gb, torch_cuda):
+    rng = np.random.default_rng(5)
+    sizes = np.round(np.exp(rng.uniform(np.log(64), np.log(1024), 24))).astype(int)
+    soft = 0.04 / np.cbrt(sizes)
+    tol, tf = 1e-9, 0.05
+    xs, x0 = _systems(gb, sizes, 100)
+    ref = gb.Batch("DOPRI5", sizes, soft, precision="f64")
+    ref.start(x0, 0.0, tf, tol, tol)
+    assert ref.advance() == 0
+    xr, _ = ref.state()
+    b = gb.Batch("DOPRI5", sizes, soft, precision="mixed")
+    b.start(x0, 0.0, tf, tol, tol)
+    choice = b.autotune(2)
+    assert choice["stage_ms"] > 0
+    assert b.advance() == 0
+    xm, tm = b.state()
+    np.testing.assert_allclose(tm, tf)
+    assert (xm - xr).abs().max().item() <= 1e-6
+    ref.close()
+    b.close()
+
+
+def test_batch_budget_status(gb, torch_cuda):
+    sizes = [40, 50]
+    xs, x0 = _systems(gb, sizes, 7)
+    b = gb.Batch("DOPRI5", sizes, 0.05, precision="f64", max_attempts=3)
+    b.start(x0, 0.0, 5.0, 1e-12, 1e-12)
+    assert b.advance() == gb.GB_ERR_BUDGET
+    st = b.stats(per_system=True)
+    assert all(s["n_attempts"] == 3 for s in st["systems"])
+    b.close()
