@@ -127,6 +127,24 @@ int gb_nbody_rhs_mixed(const double* x_dev, double* dxdt_dev, int64_t n_particle
                        double softening, double mass, const double* masses_dev, void* work_dev,
                        const gb_force_tiling* tiling, gb_stream_t stream);
 
+/* No counterpart in the reference.  The same mixed-precision right-hand   */
+/* side for callers that cannot allocate device memory (a host that gives  */
+/* the library a fixed slice of device memory and refuses further          */
+/* cudaMalloc, or a per-stage caller that cannot pay for cudaMalloc /      */
+/* cudaFree, whose free waits for the whole device).  The workspace is a   */
+/* fixed array inside the library (2 MiB + 256 B per GPU that loads it,    */
+/* held until exit), so n_particles may not exceed                         */
+/* gb_nbody_rhs_mixed_noalloc_max_bodies() (65536); larger n returns       */
+/* GB_ERR_CAPACITY.  The first call on each device looks the array's       */
+/* device address up (cudaGetSymbolAddress); make that first call before   */
+/* any stream capture.  All calls share the one array, so calls that       */
+/* overlap on the GPU (other streams, other threads) race and must be      */
+/* serialised by the caller.  Nothing in it needs to start at zero.        */
+int64_t gb_nbody_rhs_mixed_noalloc_max_bodies(void);
+int gb_nbody_rhs_mixed_noalloc(const double* x_dev, double* dxdt_dev, int64_t n_particles,
+                               double softening, double mass, const double* masses_dev,
+                               const gb_force_tiling* tiling, gb_stream_t stream);
+
 /* ---------------------------------------------------------------------- */
 /* Element-wise embedded-RK kernels with a host-scalar dt.                 */
 /* ---------------------------------------------------------------------- */

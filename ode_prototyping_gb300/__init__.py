@@ -122,6 +122,9 @@ SIGNATURES = {
     "gb_nbody_mixed_workspace_bytes": (C.c_size_t, [_I64]),
     "gb_nbody_rhs_mixed": (C.c_int, [_DP, _DP, _I64, _D, _D, _DP, _VP, C.POINTER(GbForceTiling),
                                      _VP]),
+    "gb_nbody_rhs_mixed_noalloc_max_bodies": (C.c_int64, []),
+    "gb_nbody_rhs_mixed_noalloc": (C.c_int, [_DP, _DP, _I64, _D, _D, _DP,
+                                             C.POINTER(GbForceTiling), _VP]),
     "gb_rk_stage_f64": (C.c_int, [C.POINTER(GbTableau), _I32, _D, _DP, _DP, _DP, _I64, _VP]),
     "gb_rk_update_state_and_error_f64": (C.c_int, [C.POINTER(GbTableau), _D, _DP, _DP, _DP, _DP,
                                                    _I64, _VP]),

@@ -289,6 +289,36 @@ extern "C" int gb_nbody_acc_f64(const double* pos, double* acc, int64_t n, doubl
                  accumulate ? kModeAccAdd : kModeAccWrite, tiling, as_cuda(stream));
 }
 
+namespace gb {
+// Mixed-precision right-hand side into caller-located scratch: `packed`
+// (n PackedBody records, 16-byte aligned) and `c` (3 doubles).  Same kernels
+// and launch geometry as gb_nbody_rhs_mixed; allocates nothing.
+int mixed_rhs_into(const double* x, double* dxdt, long long n, double softening, double mass,
+                   const double* masses, PackedBody* packed, double* c,
+                   const gb_force_tiling* tiling, cudaStream_t s) {
+  centroid_kernel<<<1, 1024, 0, s>>>(x, n, c);
+  GB_CUDA_TRY(cudaGetLastError());
+  pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, masses, c, n, packed);
+  GB_CUDA_TRY(cudaGetLastError());
+  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
+  const void* k = nullptr;
+  switch (g.T) {
+    case 64: k = pick_mixed<64>(g.L, g.BPT); break;
+    case 128: k = pick_mixed<128>(g.L, g.BPT); break;
+    case 256: k = pick_mixed<256>(g.L, g.BPT); break;
+  }
+  if (!k) return GB_ERR_UNSUPPORTED;
+  const double* vel = x + 3 * n;
+  double* out_vel = dxdt;
+  double* out_acc = dxdt + 3 * n;
+  float eps2 = (float)(softening * softening);
+  int uniform = masses ? 0 : 1;
+  void* args[] = {(void*)&packed, (void*)&vel,  (void*)&out_vel, (void*)&out_acc,
+                  (void*)&n,      (void*)&eps2, (void*)&mass,    (void*)&uniform};
+  return launch_cluster(k, g, 0, s, args);
+}
+}  // namespace gb
+
 extern "C" size_t gb_nbody_mixed_workspace_bytes(int64_t n) {
   if (n < 1) return 0;
   // packed bodies + reference point (3 doubles), 256-byte aligned pieces
