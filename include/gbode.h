@@ -127,6 +127,19 @@ int gb_nbody_rhs_mixed(const double* x_dev, double* dxdt_dev, int64_t n_particle
                        double softening, double mass, const double* masses_dev, void* work_dev,
                        const gb_force_tiling* tiling, gb_stream_t stream);
 
+/* The same mixed-precision right-hand side on spatially sorted tiles: the */
+/* bodies are ordered along a Morton curve, every 128-body tile carries its */
+/* centroid and radius, and partners in a tile whose gap to the i-tile is   */
+/* at least that tile's radius use FP32 coordinates relative to the tile    */
+/* centroid (one subtraction per component; relative error <= 4 * 2^-24);  */
+/* nearer tiles use the hi/lo difference.  Rows are returned in body order. */
+/* work_dev: gb_nbody_mixed_sorted_workspace_bytes(n) bytes, 256-aligned.   */
+size_t gb_nbody_mixed_sorted_workspace_bytes(int64_t n_particles);
+int gb_nbody_rhs_mixed_sorted(const double* x_dev, double* dxdt_dev, int64_t n_particles,
+                              double softening, double mass, const double* masses_dev,
+                              void* work_dev, size_t work_bytes, const gb_force_tiling* tiling,
+                              gb_stream_t stream);
+
 /* No counterpart in the reference.  The same mixed-precision right-hand   */
 /* side for callers that cannot allocate device memory (a host that gives  */
 /* the library a fixed slice of device memory and refuses further          */
@@ -279,7 +292,8 @@ typedef struct {
   gb_force_tiling tiling;     /* 0 fields = auto */
   const void* mlp;            /* gb_mlp* weights for GB_CTRL_LEARNED (device-resident copy made) */
   int32_t log_steps;          /* record per-attempt controller logs on the device */
-  int32_t reserved;
+  int32_t spatial_sort;       /* mixed precision: Morton-sorted tiles with the far-field
+                                 path (0 = on, -1 = off) */
 } gb_integrate_opts;
 
 typedef struct {

@@ -63,7 +63,7 @@ class GbIntegrateOpts(C.Structure):
                 ("exact", C.c_int32), ("attempts_per_sync", C.c_int32), ("record", C.c_int32),
                 ("max_attempts", C.c_int64), ("host_wait_timeout_s", C.c_double),
                 ("pi_beta", C.c_double), ("tiling", GbForceTiling), ("mlp", C.c_void_p),
-                ("log_steps", C.c_int32), ("reserved", C.c_int32)]
+                ("log_steps", C.c_int32), ("spatial_sort", C.c_int32)]
 
 
 class GbIntegrateStats(C.Structure):
@@ -122,6 +122,9 @@ SIGNATURES = {
     "gb_nbody_mixed_workspace_bytes": (C.c_size_t, [_I64]),
     "gb_nbody_rhs_mixed": (C.c_int, [_DP, _DP, _I64, _D, _D, _DP, _VP, C.POINTER(GbForceTiling),
                                      _VP]),
+    "gb_nbody_mixed_sorted_workspace_bytes": (C.c_size_t, [_I64]),
+    "gb_nbody_rhs_mixed_sorted": (C.c_int, [_DP, _DP, _I64, _D, _D, _DP, _VP, C.c_size_t,
+                                            C.POINTER(GbForceTiling), _VP]),
     "gb_nbody_rhs_mixed_noalloc_max_bodies": (C.c_int64, []),
     "gb_nbody_rhs_mixed_noalloc": (C.c_int, [_DP, _DP, _I64, _D, _D, _DP,
                                              C.POINTER(GbForceTiling), _VP]),
@@ -291,6 +294,23 @@ def nbody_rhs_mixed(x, n_particles: int, softening: float, mass: float = 1.0, ma
     return out
 
 
+def nbody_rhs_mixed_sorted(x, n_particles: int, softening: float, mass: float = 1.0,
+                           masses=None, tile: GbForceTiling | None = None, out=None,
+                           stream=None):
+    """Mixed-precision RHS on Morton-sorted tiles with the far-field path."""
+    torch = _torch()
+    x = to_device(x)
+    out = out if out is not None else torch.empty_like(x)
+    nb = lib().gb_nbody_mixed_sorted_workspace_bytes(n_particles)
+    work = torch.empty(nb + 256, dtype=torch.uint8, device="cuda")
+    base = (work.data_ptr() + 255) // 256 * 256
+    check(lib().gb_nbody_rhs_mixed_sorted(_ptr(x), _ptr(out), n_particles, softening, mass,
+                                          _ptr(masses), base, nb,
+                                          C.byref(tile) if tile else None, _stream(stream)),
+          "gb_nbody_rhs_mixed_sorted")
+    return out
+
+
 def energy(x, n_particles: int, softening: float, mass: float = 1.0, masses=None, stream=None):
     torch = _torch()
     x = to_device(x)
@@ -431,6 +451,7 @@ class Gb300Executor:
     pi_beta: float = 0.04
     mlp: GbMlp | None = None
     log_steps: int = 0
+    spatial_sort: bool = True
 
     def rhs(self, ode: NBodyODE, x, dxdt):
         if self.precision == "f64":
@@ -457,6 +478,7 @@ class Gb300Executor:
             self._mlp_keep = self.mlp
             o.mlp = C.cast(C.pointer(self.mlp), C.c_void_p)
         o.log_steps = self.log_steps
+        o.spatial_sort = 0 if self.spatial_sort else -1
         return o
 
 

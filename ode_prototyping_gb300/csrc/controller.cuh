@@ -2,6 +2,7 @@
 // of every attempt (no host round trip).
 #pragma once
 
+#include "ddpow.cuh"
 #include "integrator.cuh"
 #include "mlp.cuh"
 
@@ -14,8 +15,9 @@ constexpr double kMinStepScale = 0.33;  // RKEmbeddedParallel.hpp:22
 // dtnew = dt * safety / err^(1/(1+q)), clamped to x6 / x0.33, with a floor
 // at (tf - t0) * 1e-12 reached only inside the clamp window.
 __device__ __forceinline__ double reference_step(double dt, double err, double safety, int q,
-                                                 double t0, double tf) {
-  const double dtnew = dt * safety / pow(err, 1.0 / (1.0 + q));
+                                                 double t0, double tf, bool exact_pow) {
+  const double e = 1.0 / (1.0 + q);
+  const double dtnew = dt * safety / (exact_pow ? dd_pow(err, e) : pow(err, e));
   if (fabs(dtnew) > kMaxStepScale * fabs(dt)) return dt * kMaxStepScale;
   if (fabs(dtnew) < kMinStepScale * fabs(dt)) return dt * kMinStepScale;
   if (dtnew / (tf - t0) < 1.0e-12) return (tf - t0) * 1.0e-12;
@@ -123,9 +125,14 @@ __device__ inline void finish_attempt(const DevTableau& tab, const CtrlEnv& P, C
     dtn = pi_step(c, dt, err, accepted);
   } else if (c.controller == GB_CTRL_LEARNED) {
     if (accepted && have_learned) {
-      // The network proposes the next step; the embedded error estimate of
-      // that attempt still decides acceptance.
-      double scale = exp(fmin(fmax(learned_log_scale, -1.1), 1.79));  // within [0.33, 6.0]
+      // The network proposes a correction to the elementary controller's
+      // log step ratio log(safety) - log(err) / (1 + q); the embedded error
+      // estimate of the next attempt still decides acceptance.
+      const double base =
+          err > 0.0 ? log(c.safety) - log(err) / (1.0 + c.q) : log(kMaxStepScale);
+      const double lg = fmin(fmax(base + learned_log_scale, log(kMinStepScale)),
+                             log(kMaxStepScale));
+      double scale = exp(lg);
       if (c.reject_prev) scale = fmin(scale, 1.0);
       dtn = dt * scale;
       c.learned_dt = dtn;
@@ -137,7 +144,7 @@ __device__ inline void finish_attempt(const DevTableau& tab, const CtrlEnv& P, C
       dtn = pi_step(c, dt, err, accepted);  // fallback on every rejection
     }
   } else {
-    dtn = reference_step(dt, err, c.safety, c.q, c.t0, c.tf);
+    dtn = reference_step(dt, err, c.safety, c.q, c.t0, c.tf, c.exact_pow != 0);
   }
   c.dt = dtn;
   if (c.t + c.dt > c.tf) c.dt = c.tf - c.t;

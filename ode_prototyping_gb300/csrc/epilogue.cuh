@@ -19,6 +19,30 @@ __device__ __forceinline__ int kslot(int l, int S, int k0slot) {
   return l;
 }
 
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = dadd(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st /= 2) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
 struct EpiCtx {
   const DevTableau* tab;
   int s, S, k0slot;
@@ -46,7 +70,8 @@ struct EpiCtx {
 // sq_acc (last stage) and its |a| to amax (stage 0).
 template <int PREC>
 __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, const double* acc,
-                                              double& sq_acc, double& amax) {
+                                              double& sq_acc, double& amax,
+                                              double* newpos = nullptr) {
   const DevTableau& tab = *E.tab;
   const int s = E.s, S = E.S;
   const long long n = E.n;
@@ -85,7 +110,11 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
       yn[e] = dadd(E.x0[idx[e]], dmul(v, E.dt));
       E.ynext[idx[e]] = yn[e];
     }
-    if constexpr (PREC == GB_PREC_MIXED) {
+    if (newpos) {
+      newpos[0] = yn[0];
+      newpos[1] = yn[1];
+      newpos[2] = yn[2];
+    } else if constexpr (PREC == GB_PREC_MIXED) {
       const float w = E.masses ? (float)E.masses[i] : 1.0f;
       E.pnext[i] = pack_body(yn[0], yn[1], yn[2], E.cref[0], E.cref[1], E.cref[2], w);
     }
@@ -117,35 +146,54 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
         sq_acc = dadd(sq_acc, sq);
       }
     }
-    if constexpr (PREC == GB_PREC_MIXED) {
+    if (newpos) {
+      newpos[0] = xn[0];
+      newpos[1] = xn[1];
+      newpos[2] = xn[2];
+    } else if constexpr (PREC == GB_PREC_MIXED) {
       const float w = E.masses ? (float)E.masses[i] : 1.0f;
       E.pnext[i] = pack_body(xn[0], xn[1], xn[2], E.cref[0], E.cref[1], E.cref[2], w);
     }
   }
 }
 
-__device__ __forceinline__ double block_sum(double v, double* red) {
-  red[threadIdx.x] = v;
-  __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st /= 2) {
-    if ((int)threadIdx.x < st) red[threadIdx.x] = dadd(red[threadIdx.x], red[threadIdx.x + st]);
-    __syncthreads();
+// Packs one sorted tile whose bodies' new positions are held one per thread
+// (threadIdx.x < cnt): FP64 centroid and radius by block reductions, then the
+// near record (hi/lo of x - c), the far record (FP32 x - c_J, weight) and the
+// tile metadata.  All threads of the CTA must call it.
+__device__ __forceinline__ void pack_sorted_tile(const double* p, bool valid, int cnt, float w,
+                                                 const double* cref, PackedBody* near_out,
+                                                 float4* far_out, TileMeta* meta_out,
+                                                 double* red) {
+  double c[3];
+  for (int d = 0; d < 3; ++d) c[d] = block_sum(valid ? p[d] : 0.0, red) / (double)cnt;
+  double r2 = 0.0;
+  if (valid) {
+    const double dx = p[0] - c[0], dy = p[1] - c[1], dz = p[2] - c[2];
+    r2 = dx * dx + dy * dy + dz * dz;
   }
-  double r = red[0];
-  __syncthreads();
-  return r;
-}
-
-__device__ __forceinline__ double block_max(double v, double* red) {
-  red[threadIdx.x] = v;
-  __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st /= 2) {
-    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
-    __syncthreads();
+  const double rad = sqrt(block_max(r2, red));
+  if (valid) {
+    *near_out = pack_body(p[0], p[1], p[2], cref[0], cref[1], cref[2], w);
+    *far_out = make_float4(__double2float_rn(p[0] - c[0]), __double2float_rn(p[1] - c[1]),
+                           __double2float_rn(p[2] - c[2]), w);
   }
-  double r = red[0];
-  __syncthreads();
-  return r;
+  if (threadIdx.x == 0) {
+    TileMeta m;
+    float h, l;
+    split_hilo(c[0] - cref[0], h, l);
+    m.chi.x = h;
+    m.clo.x = l;
+    split_hilo(c[1] - cref[1], h, l);
+    m.chi.y = h;
+    m.clo.y = l;
+    split_hilo(c[2] - cref[2], h, l);
+    m.chi.z = h;
+    m.clo.z = l;
+    m.chi.w = __double2float_ru(rad * (1.0 + 1e-6));
+    m.clo.w = 0.f;
+    *meta_out = m;
+  }
 }
 
 }  // namespace gb

@@ -243,6 +243,145 @@ __device__ __forceinline__ void force_mixed_cta(const PackedBody* __restrict__ p
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision on spatially sorted bodies.  Bodies are processed in a
+// Morton order, so consecutive 128-body tiles are compact.  Each j-tile J
+// carries its centroid c_J (hi/lo FP32 parts of c_J - c) and radius R_J, and
+// each body a second record: FP32 (x_j - c_J).  For a j-tile whose gap to the
+// CTA's i-tile is at least R_J, the pair difference is one subtraction per
+// component, dx = (x_j - c_J) - (x_i - c_J), with x_i - c_J formed once per
+// tile from the i-body's hi/lo parts; its error is at most
+// 2^-24 (R_J + |x_i - c_J| + |dx|) <= 2^-24 (2 R_J + 2|dx|) <= 4 * 2^-24 |dx|.
+// Tiles closer than that use the hi/lo difference of force_mixed_cta.
+// ---------------------------------------------------------------------------
+struct TileMeta {
+  float4 chi;  // hi parts of c_J - c, radius R_J in .w
+  float4 clo;  // lo parts of c_J - c
+};
+
+// far when the gap between the two tiles' bounding spheres is >= 1.1 R_J
+__device__ __forceinline__ bool tile_is_far(const TileMeta& I, const TileMeta& J) {
+  const float dx = (J.chi.x - I.chi.x) + (J.clo.x - I.clo.x);
+  const float dy = (J.chi.y - I.chi.y) + (J.clo.y - I.clo.y);
+  const float dz = (J.chi.z - I.chi.z) + (J.clo.z - I.clo.z);
+  const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+  return d - I.chi.w - J.chi.w >= 1.1f * J.chi.w;
+}
+
+template <int T, int L, int BPT, bool UNIFORM>
+__device__ __forceinline__ void force_mixed_sorted_cta(
+    const PackedBody* __restrict__ near, const float4* __restrict__ far,
+    const TileMeta* __restrict__ meta, long long n, long long itile, long long jb, long long je,
+    float eps2, PackedBody* sh, double (*part)[3]) {
+  constexpr int BG = T / L;
+  constexpr int BI = BG * BPT;
+  static_assert(BI == T, "sorted tiles: i-tile and j-tile sizes must match");
+  const int g = threadIdx.x / L;
+  const int l = threadIdx.x % L;
+  const long long i0 = itile * BI;
+  float hx[BPT], hy[BPT], hz[BPT], lx[BPT], ly[BPT], lz[BPT];
+  float sx[BPT], sy[BPT], sz[BPT], cx[BPT], cy[BPT], cz[BPT];
+#pragma unroll
+  for (int q = 0; q < BPT; ++q) {
+    const long long i = i0 + (long long)q * BG + g;
+    PackedBody pb;
+    if (i < n) {
+      pb = near[i];
+    } else {
+      pb.hw = make_float4(1e30f, 1e30f, 1e30f, 0.f);  // far from everything, weight 0
+      pb.lo = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    hx[q] = pb.hw.x; hy[q] = pb.hw.y; hz[q] = pb.hw.z;
+    lx[q] = pb.lo.x; ly[q] = pb.lo.y; lz[q] = pb.lo.z;
+    sx[q] = sy[q] = sz[q] = 0.f;
+    cx[q] = cy[q] = cz[q] = 0.f;
+  }
+  const TileMeta mi = meta[itile];
+  constexpr int JT = T;
+  for (long long j0 = jb; j0 < je; j0 += JT) {
+    const int cnt = (int)min((long long)JT, je - j0);
+    const TileMeta mj = meta[j0 / JT];
+    const bool is_far = tile_is_far(mi, mj);
+    __syncthreads();
+    if (is_far) {
+      float4* dst = reinterpret_cast<float4*>(sh);
+      for (int k = threadIdx.x; k < cnt; k += T) dst[k] = far[j0 + k];
+    } else {
+      const float4* src = reinterpret_cast<const float4*>(near + j0);
+      float4* dst = reinterpret_cast<float4*>(sh);
+      for (int k = threadIdx.x; k < 2 * cnt; k += T) dst[k] = src[k];
+    }
+    __syncthreads();
+    float tx[BPT], ty[BPT], tz[BPT];
+#pragma unroll
+    for (int q = 0; q < BPT; ++q) tx[q] = ty[q] = tz[q] = 0.f;
+    if (is_far) {
+      float rx[BPT], ry[BPT], rz[BPT];
+#pragma unroll
+      for (int q = 0; q < BPT; ++q) {  // x_i - c_J, once per tile
+        rx[q] = (hx[q] - mj.chi.x) + (lx[q] - mj.clo.x);
+        ry[q] = (hy[q] - mj.chi.y) + (ly[q] - mj.clo.y);
+        rz[q] = (hz[q] - mj.chi.z) + (lz[q] - mj.clo.z);
+      }
+      const float4* shf = reinterpret_cast<const float4*>(sh);
+#pragma unroll 4
+      for (int jj = l; jj < cnt; jj += L) {
+        const float4 pj = shf[jj];
+#pragma unroll
+        for (int q = 0; q < BPT; ++q) {
+          const float dx = pj.x - rx[q];
+          const float dy = pj.y - ry[q];
+          const float dz = pj.z - rz[q];
+          const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+          const float rinv = rsqrt_sfu(r2);
+          const float s = UNIFORM ? rinv * (rinv * rinv) : (pj.w * rinv) * (rinv * rinv);
+          tx[q] = fmaf(s, dx, tx[q]);
+          ty[q] = fmaf(s, dy, ty[q]);
+          tz[q] = fmaf(s, dz, tz[q]);
+        }
+      }
+    } else {
+#pragma unroll 4
+      for (int jj = l; jj < cnt; jj += L) {
+        const float4 hw = sh[jj].hw;
+        const float4 lo = sh[jj].lo;
+#pragma unroll
+        for (int q = 0; q < BPT; ++q) {
+          const float dx = (hw.x - hx[q]) + (lo.x - lx[q]);
+          const float dy = (hw.y - hy[q]) + (lo.y - ly[q]);
+          const float dz = (hw.z - hz[q]) + (lo.z - lz[q]);
+          const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+          const float rinv = rsqrt_sfu(r2);
+          const float s = UNIFORM ? rinv * (rinv * rinv) : (hw.w * rinv) * (rinv * rinv);
+          tx[q] = fmaf(s, dx, tx[q]);
+          ty[q] = fmaf(s, dy, ty[q]);
+          tz[q] = fmaf(s, dz, tz[q]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < BPT; ++q) {
+      kahan_add(sx[q], cx[q], tx[q]);
+      kahan_add(sy[q], cy[q], ty[q]);
+      kahan_add(sz[q], cz[q], tz[q]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < BPT; ++q) {
+    double ax = dsub((double)sx[q], (double)cx[q]);
+    double ay = dsub((double)sy[q], (double)cy[q]);
+    double az = dsub((double)sz[q], (double)cz[q]);
+    ax = lane_reduce<L>(ax);
+    ay = lane_reduce<L>(ay);
+    az = lane_reduce<L>(az);
+    if (l == 0) {
+      part[q * BG + g][0] = ax;
+      part[q * BG + g][1] = ay;
+      part[q * BG + g][2] = az;
+    }
+  }
+}
+
 // Packs FP64 positions (and optional per-body masses) into PackedBody
 // records relative to the reference point c.
 __device__ __forceinline__ PackedBody pack_body(double x, double y, double z, double cx,

@@ -24,6 +24,7 @@
 #include "controller.cuh"
 #include "epilogue.cuh"
 #include "mlp.cuh"
+#include "sortpack.cuh"
 
 namespace gb {
 
@@ -106,6 +107,95 @@ __global__ void __launch_bounds__(T)
   double sq_acc = 0.0;
   double amax = 0.0;
   for (int b = threadIdx.x; b < nb; b += T) body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
+  if (s == 0 && !skip_force) {
+    const double m = block_max(amax, red);
+    if (threadIdx.x == 0) P.aux[ci.itile] = m;
+  }
+  if (!last) return;
+  const double tile_sum = block_sum(sq_acc, red);
+  if (threadIdx.x == 0) P.partials[ci.itile] = tile_sum;
+}
+
+// The mixed-precision stage on Morton-sorted tiles: i-tile = 128 consecutive
+// sorted bodies, far j-tiles through the tile-centroid records, the epilogue
+// repacks the CTA's own tile (centroid, radius, near and far records) for
+// the next stage.
+template <int T, int L, int BPT, bool UNIFORM>
+__global__ void __launch_bounds__(T, 1024 / T)
+    fused_sorted_kernel(const __grid_constant__ DevTableau tab,
+                        const __grid_constant__ FusedParams P, int s) {
+  constexpr int BI = (T / L) * BPT;
+  static_assert(BI == T, "one body per thread in the epilogue");
+  __shared__ __align__(16) PackedBody sh[T];
+  __shared__ double part[BI][3];
+  __shared__ double red[T];
+  Ctrl* C = P.ctrl;
+  if (C->done) return;
+  const int cur = C->cur;
+  const double dt = C->dt;
+  const int k0_valid = C->k0_valid;
+  const int k0slot = C->k0slot;
+  const int px = C->px;
+  const int S = tab.n_stages;
+  const long long n = P.n, n_var = P.n_var, nt = P.n_itiles;
+  const double* x0 = P.ring + (long long)cur * n_var;
+  const double* ysrc = (s == 0) ? x0 : P.Y + (long long)(s & 1) * n_var;
+  const ClusterInfo ci = cluster_info();
+  const long long i0 = ci.itile * BI;
+  const bool skip_force = (s == 0 && k0_valid);
+  if (!skip_force) {
+    long long jb, je;
+    j_chunk(n, ci.rank, ci.size, T, jb, je);
+    const PackedBody* near = (s == 0) ? P.PX + (long long)px * n : P.PY + (long long)(s & 1) * n;
+    const float4* far = (s == 0) ? P.PXF + (long long)px * n : P.PYF + (long long)(s & 1) * n;
+    const TileMeta* meta = (s == 0) ? P.MX + (long long)px * nt : P.MY + (long long)(s & 1) * nt;
+    force_mixed_sorted_cta<T, L, BPT, UNIFORM>(near, far, meta, n, ci.itile, jb, je, P.eps2f, sh,
+                                               part);
+    cluster_combine<BI>(part, ci.rank, ci.size);
+  }
+  if (ci.rank != 0) return;
+  const bool last = (s == S - 1);
+  EpiCtx E;
+  E.tab = &tab;
+  E.s = s;
+  E.S = S;
+  E.k0slot = k0slot;
+  E.skip_force = skip_force;
+  E.last = last;
+  E.exact = false;
+  E.dt = dt;
+  E.n = n;
+  E.x0 = x0;
+  E.ysrc = ysrc;
+  E.ks = P.ks;
+  E.kstride = n_var;
+  E.ynext = P.Y + (long long)((s + 1) & 1) * n_var;
+  E.xnew = P.ring + (long long)((cur + 1) % P.R) * n_var;
+  E.pnext = nullptr;
+  E.atol = P.atol;
+  E.rtol = P.rtol;
+  E.atol_s = P.atol_s;
+  E.rtol_s = P.rtol_s;
+  E.masses = P.masses;
+  E.mass = P.mass;
+  E.cref = P.cref;
+  E.sq = nullptr;
+  const long long nb = min((long long)BI, n - i0);
+  const int b = threadIdx.x;
+  const bool valid = b < nb;
+  double np[3] = {0.0, 0.0, 0.0};
+  double sq_acc = 0.0, amax = 0.0;
+  long long id = 0;
+  if (valid) {
+    id = P.perm[i0 + b];
+    body_epilogue<GB_PREC_MIXED>(E, id, part[b], sq_acc, amax, np);
+  }
+  const long long po = last ? (long long)(px ^ 1) : (long long)((s + 1) & 1);
+  PackedBody* near_out = (last ? P.PX : P.PY) + po * n + i0 + b;
+  float4* far_out = (last ? P.PXF : P.PYF) + po * n + i0 + b;
+  TileMeta* meta_out = (last ? P.MX : P.MY) + po * nt + ci.itile;
+  const float w = valid ? (P.masses ? (float)P.masses[id] : 1.0f) : 0.f;
+  pack_sorted_tile(np, valid, (int)nb, w, P.cref, near_out, far_out, meta_out, red);
   if (s == 0 && !skip_force) {
     const double m = block_max(amax, red);
     if (threadIdx.x == 0) P.aux[ci.itile] = m;
@@ -257,7 +347,7 @@ __global__ void centroid_state_kernel(const double* __restrict__ x, long long n,
 __global__ void init_ctrl_kernel(Ctrl* C, const double* __restrict__ d, double t0, double tf,
                                  double* times_ring, int p, int q, double safety,
                                  int controller, double pi_beta, int fsal,
-                                 long long max_attempts) {
+                                 long long max_attempts, int exact) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const double d0 = d[0], d1 = d[1];
   const double dt0 = initial_dt0(d0, d1);
@@ -268,11 +358,12 @@ __global__ void init_ctrl_kernel(Ctrl* C, const double* __restrict__ d, double t
     const double alt = dt0 * 1.0e-3;
     dt1 = alt < 1.0e-6 ? 1.0e-6 : alt;
   } else {
-    dt1 = pow(0.01 / dmax, 1.0 / (1.0 + p));
+    dt1 = exact ? dd_pow(0.01 / dmax, 1.0 / (1.0 + p)) : pow(0.01 / dmax, 1.0 / (1.0 + p));
   }
   const double big = 100.0 * dt0;
   Ctrl c;
   memset(&c, 0, sizeof c);
+  c.exact_pow = exact;
   c.t = t0;
   c.t0 = t0;
   c.tf = tf;
@@ -353,6 +444,19 @@ const void* pick_fused(int prec, int T, int L, int BPT) {
   return nullptr;
 }
 
+template <int T, int L, bool U>
+const void* sorted_ptr() {
+  return (const void*)fused_sorted_kernel<T, L, L, U>;
+}
+
+const void* pick_sorted(int T, int L, bool uniform) {
+#define GB_SK(T_, L_)                                                        \
+  if (T == T_ && L == L_) return uniform ? sorted_ptr<T_, L_, true>() : sorted_ptr<T_, L_, false>();
+  GB_SK(128, 1) GB_SK(128, 2) GB_SK(256, 1) GB_SK(256, 2)
+#undef GB_SK
+  return nullptr;
+}
+
 }  // namespace
 
 // Standalone RHS used by the start-up (initial step) path.
@@ -399,6 +503,19 @@ struct gb_integrator_s {
   double* masses = nullptr;
   gb::StepLog* log = nullptr;
   long long log_capacity = 0;
+  // spatially sorted mixed path
+  bool sorted = false;
+  int* perm = nullptr;
+  int* vals = nullptr;
+  unsigned long long* keys = nullptr;
+  unsigned long long* keys_alt = nullptr;
+  void* cub_temp = nullptr;
+  size_t cub_bytes = 0;
+  double* bbox = nullptr;
+  float4* PXF = nullptr;
+  float4* PYF = nullptr;
+  gb::TileMeta* MX = nullptr;
+  gb::TileMeta* MY = nullptr;
   void* mlp_dev = nullptr;
   // host
   gb::Ctrl* hctrl = nullptr;  // pinned
@@ -433,7 +550,9 @@ void free_all(gb_integrator_s* it) {
   if (it->graph) cudaGraphDestroy(it->graph);
   void* bufs[] = {it->ctrl,  it->ring, it->times_ring, it->ks,     it->Y,        it->PX,
                   it->PY,    it->atol, it->rtol,       it->cref,   it->partials, it->aux,
-                  it->sq,    it->dscal, it->norm_work, it->masses, it->log,      it->mlp_dev};
+                  it->sq,    it->dscal, it->norm_work, it->masses, it->log,      it->mlp_dev,
+                  it->perm,  it->vals, it->keys,     it->keys_alt, it->cub_temp, it->bbox,
+                  it->PXF,   it->PYF,  it->MX,       it->MY};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (it->hctrl) cudaFreeHost(it->hctrl);
@@ -451,9 +570,24 @@ int launch_fused(gb_integrator_s* it, int s) {
   return GB_OK;
 }
 
+// Re-sorts the bodies of x0 along a Morton curve and repacks x0's tiles.
+int launch_resort(gb_integrator_s* it) {
+  if (!it->sorted) return GB_OK;
+  cudaStream_t s = it->stream;
+  const long long n = it->n;
+  const int* cur = reinterpret_cast<const int*>(reinterpret_cast<const char*>(it->ctrl) +
+                                                offsetof(Ctrl, cur));
+  const int* px = reinterpret_cast<const int*>(reinterpret_cast<const char*>(it->ctrl) +
+                                               offsetof(Ctrl, px));
+  SortBuffers sb{it->perm, it->vals, it->keys, it->keys_alt, it->cub_temp, it->cub_bytes,
+                 it->bbox};
+  return sort_and_pack(it->ring, cur, it->n_var, n, sb, it->masses, it->cref, it->PX, it->PXF,
+                       it->MX, px, it->geom.n_itiles, it->geom.T, s);
+}
+
 int build_graph(gb_integrator_s* it) {
   GB_CUDA_TRY(cudaStreamBeginCapture(it->stream, cudaStreamCaptureModeThreadLocal));
-  int rc = GB_OK;
+  int rc = launch_resort(it);
   for (int a = 0; a < it->A && rc == GB_OK; ++a)
     for (int s = 0; s < it->S && rc == GB_OK; ++s) rc = launch_fused(it, s);
   cudaGraph_t g = nullptr;
@@ -541,8 +675,15 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   it->geom = choose_geom(it->n, opts.precision, &opts.tiling, opts.exact);
   if (opts.precision == GB_PREC_F64) it->geom.BPT = 1;
   if (opts.precision == GB_PREC_MIXED && it->geom.T < 128) it->geom.T = 128;
+  // spatially sorted tiles (mixed precision): on unless switched off
+  it->sorted = opts.precision == GB_PREC_MIXED && opts.spatial_sort >= 0;
+  if (it->sorted) {
+    if (it->geom.L > 2) it->geom.L = 2;
+    it->geom.BPT = it->geom.L;  // i-tile = j-tile = T bodies
+  }
   it->geom.n_itiles = (it->n + it->geom.bodies_per_cta() - 1) / it->geom.bodies_per_cta();
-  it->kernel = pick_fused(opts.precision, it->geom.T, it->geom.L, it->geom.BPT);
+  it->kernel = it->sorted ? pick_sorted(it->geom.T, it->geom.L, sys->masses_dev == nullptr)
+                          : pick_fused(opts.precision, it->geom.T, it->geom.L, it->geom.BPT);
   int rc = GB_OK;
   auto fail = [&](int code) {
     free_all(it);
@@ -582,6 +723,19 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
       note_cuda_error(e);
       return fail(GB_ERR_CUDA);
     }
+  }
+  if (it->sorted) {
+    GB_ALLOC(it->perm, (size_t)n * sizeof(int));
+    GB_ALLOC(it->vals, (size_t)n * sizeof(int));
+    GB_ALLOC(it->keys, (size_t)n * sizeof(unsigned long long));
+    GB_ALLOC(it->keys_alt, (size_t)n * sizeof(unsigned long long));
+    GB_ALLOC(it->bbox, 8 * sizeof(double));
+    GB_ALLOC(it->PXF, (size_t)2 * n * sizeof(float4));
+    GB_ALLOC(it->PYF, (size_t)2 * n * sizeof(float4));
+    GB_ALLOC(it->MX, (size_t)2 * it->geom.n_itiles * sizeof(TileMeta));
+    GB_ALLOC(it->MY, (size_t)2 * it->geom.n_itiles * sizeof(TileMeta));
+    it->cub_bytes = sort_temp_bytes(n);
+    GB_ALLOC(it->cub_temp, it->cub_bytes);
   }
   if (opts.log_steps > 0) {
     it->log_capacity = opts.log_steps;
@@ -638,6 +792,11 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   P.n_itiles = it->geom.n_itiles;
   P.exact = opts.exact;
   P.S = it->S;
+  P.perm = it->perm;
+  P.PXF = it->PXF;
+  P.PYF = it->PYF;
+  P.MX = it->MX;
+  P.MY = it->MY;
   *out = it;
   return GB_OK;
 }
@@ -718,10 +877,11 @@ extern "C" int gb_integrator_start(gb_integrator it, const double* x0, double t0
   const double safety = std::pow(0.38, (1.0 / (1.0 + q)));
   init_ctrl_kernel<<<1, 32, 0, s>>>(it->ctrl, d, t0, tf, it->times_ring, it->htab.p, q, safety,
                                     it->opts.controller, it->opts.pi_beta, it->tab.fsal,
-                                    it->opts.max_attempts);
+                                    it->opts.max_attempts, it->opts.exact);
   GB_CUDA_TRY(cudaGetLastError());
   max_acc_kernel<<<1, 256, 0, s>>>(f0, n, it->ctrl);
   GB_CUDA_TRY(cudaGetLastError());
+  GB_TRY(launch_resort(it));
   if (!it->exec) GB_TRY(build_graph(it));
   GB_TRY(read_ctrl(it));
   it->delivered = 0;

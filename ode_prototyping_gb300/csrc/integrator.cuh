@@ -36,6 +36,7 @@ struct Ctrl {
   int q;
   int last_accepted;
   int learned_active; // the current attempt uses a learned proposal
+  int exact_pow;      // step-size formulas with the correctly rounded pow
   unsigned ticket;
   unsigned ticket2;
 };
@@ -75,6 +76,12 @@ struct FusedParams {
   long long n, n_var, n_itiles;
   int exact;
   int S;
+  // spatially sorted mixed path
+  const int* perm;       // sorted position -> body
+  float4* PXF;           // 2 * n far records (x0 / x_new)
+  float4* PYF;           // 2 * n far records (stage states)
+  TileMeta* MX;          // 2 * n_itiles tile metadata (x0 / x_new)
+  TileMeta* MY;          // 2 * n_itiles (stage states)
 };
 
 }  // namespace gb

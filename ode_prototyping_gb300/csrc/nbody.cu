@@ -4,6 +4,7 @@
 // (:68-133), which the reference runs as one thread per unordered pair with
 // six FP64 atomicAdds; here each body's sum is owned by one lane group.
 #include "force.cuh"
+#include "sortpack.cuh"
 
 namespace gb {
 
@@ -318,6 +319,121 @@ int mixed_rhs_into(const double* x, double* dxdt, long long n, double softening,
   return launch_cluster(k, g, 0, s, args);
 }
 }  // namespace gb
+
+namespace gb {
+namespace {
+
+// Mixed-precision right-hand side on Morton-sorted tiles (near hi/lo path
+// plus the tile-centroid far path); rows are written back in body order.
+template <int T, int L, bool UNIFORM>
+__global__ void __launch_bounds__(T, 1024 / T)
+    rhs_sorted_kernel(const PackedBody* __restrict__ near, const float4* __restrict__ far,
+                      const TileMeta* __restrict__ meta, const int* __restrict__ perm,
+                      const double* __restrict__ vel, double* __restrict__ out_vel,
+                      double* __restrict__ out_acc, long long n, float eps2, double mass) {
+  __shared__ __align__(16) PackedBody sh[T];
+  __shared__ double part[T][3];
+  const ClusterInfo ci = cluster_info();
+  long long jb, je;
+  j_chunk(n, ci.rank, ci.size, T, jb, je);
+  force_mixed_sorted_cta<T, L, L, UNIFORM>(near, far, meta, n, ci.itile, jb, je, eps2, sh, part);
+  cluster_combine<T>(part, ci.rank, ci.size);
+  if (ci.rank != 0) return;
+  const long long i = ci.itile * T + threadIdx.x;
+  if (i >= n) return;
+  const long long id = perm[i];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    out_vel[3 * id + c] = vel[3 * id + c];
+    out_acc[3 * id + c] = UNIFORM ? dmul(part[threadIdx.x][c], mass) : part[threadIdx.x][c];
+  }
+}
+
+struct SortedWork {
+  PackedBody* near;
+  float4* far;
+  TileMeta* meta;
+  SortBuffers sb;
+  double* cref;
+  size_t total;
+};
+
+size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+SortedWork sorted_layout(long long n, void* base) {
+  const long long nt = (n + 127) / 128;
+  char* p = static_cast<char*>(base);
+  SortedWork w;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* q = p ? p + off : nullptr;
+    off += align256(bytes);
+    return q;
+  };
+  w.near = reinterpret_cast<PackedBody*>(take((size_t)n * sizeof(PackedBody)));
+  w.far = reinterpret_cast<float4*>(take((size_t)n * sizeof(float4)));
+  w.meta = reinterpret_cast<TileMeta*>(take((size_t)nt * sizeof(TileMeta)));
+  w.sb.perm = reinterpret_cast<int*>(take((size_t)n * sizeof(int)));
+  w.sb.vals = reinterpret_cast<int*>(take((size_t)n * sizeof(int)));
+  w.sb.keys = reinterpret_cast<unsigned long long*>(take((size_t)n * 8));
+  w.sb.keys_alt = reinterpret_cast<unsigned long long*>(take((size_t)n * 8));
+  w.sb.bbox = reinterpret_cast<double*>(take(8 * sizeof(double)));
+  w.cref = reinterpret_cast<double*>(take(4 * sizeof(double)));
+  w.sb.cub_bytes = sort_temp_bytes(n);
+  w.sb.cub_temp = take(w.sb.cub_bytes);
+  w.total = off;
+  return w;
+}
+
+template <int T, int L>
+const void* pick_rhs_sorted(bool uniform) {
+  return uniform ? (const void*)rhs_sorted_kernel<T, L, true>
+                 : (const void*)rhs_sorted_kernel<T, L, false>;
+}
+
+}  // namespace
+}  // namespace gb
+
+extern "C" size_t gb_nbody_mixed_sorted_workspace_bytes(int64_t n) {
+  return n < 1 ? 0 : gb::sorted_layout(n, nullptr).total;
+}
+
+extern "C" int gb_nbody_rhs_mixed_sorted(const double* x, double* dxdt, int64_t n,
+                                         double softening, double mass, const double* masses,
+                                         void* work, size_t work_bytes,
+                                         const gb_force_tiling* tiling, gb_stream_t stream) {
+  using namespace gb;
+  GB_TRY(validate_nbody(x, dxdt, n, softening, mass, masses));
+  if (!(softening > 0.0) || !work || (reinterpret_cast<uintptr_t>(work) & 255u))
+    return GB_ERR_INVALID_ARGUMENT;
+  SortedWork w = sorted_layout(n, work);
+  if (work_bytes < w.total) return GB_ERR_CAPACITY;
+  cudaStream_t s = as_cuda(stream);
+  centroid_kernel<<<1, 1024, 0, s>>>(x, n, w.cref);
+  GB_CUDA_TRY(cudaGetLastError());
+  const long long nt = (n + 127) / 128;
+  GB_TRY(sort_and_pack(x, nullptr, 0, n, w.sb, masses, w.cref, w.near, w.far, w.meta, nullptr,
+                       nt, 128, s));
+  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
+  g.T = 128;
+  if (g.L > 2) g.L = 2;
+  g.BPT = g.L;
+  g.n_itiles = nt;
+  const void* k = g.L == 1 ? pick_rhs_sorted<128, 1>(masses == nullptr)
+                           : pick_rhs_sorted<128, 2>(masses == nullptr);
+  const PackedBody* near = w.near;
+  const float4* far = w.far;
+  const TileMeta* meta = w.meta;
+  const int* perm = w.sb.perm;
+  const double* vel = x + 3 * n;
+  double* out_vel = dxdt;
+  double* out_acc = dxdt + 3 * n;
+  float eps2 = (float)(softening * softening);
+  long long nn = n;
+  void* args[] = {(void*)&near, (void*)&far, (void*)&meta, (void*)&perm, (void*)&vel,
+                  (void*)&out_vel, (void*)&out_acc, (void*)&nn, (void*)&eps2, (void*)&mass};
+  return launch_cluster(k, g, 0, s, args);
+}
 
 extern "C" size_t gb_nbody_mixed_workspace_bytes(int64_t n) {
   if (n < 1) return 0;

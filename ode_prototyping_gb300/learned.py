@@ -6,7 +6,10 @@
 2. ``build_dataset`` pairs every accepted attempt k with the next attempt
    k+1 and sets the target to the step change that would have put attempt
    k+1 at the error ratio rho under the local error model err ~ dt^(q+1):
-   r_k = log(dt_{k+1} (rho / err_{k+1})^(1/(q+1))) - log(dt_k).
+   r_k = log(dt_{k+1} (rho / err_{k+1})^(1/(q+1))) - log(dt_k), minus the
+   elementary controller's own proposal log(safety) - log(err_k)/(q+1): the
+   network learns a correction to the reference's step-size formula, so
+   features outside the training range fall back towards that formula.
 3. ``train`` fits the 16 -> 64 -> 64 -> 1 SiLU network with the library's
    own forward / backward / Adam kernels (``gb_mlp_train``), asymmetric loss
    (over-long steps cost a rejected attempt, so over-prediction weighs more).
@@ -31,12 +34,13 @@ FEAT, LOG_DT, LOG_ERR, ACCEPTED = slice(0, 16), 16, 17, 18
 
 
 def collect_logs(seeds, n: int, softening: float, tab: str, tol: float, tf: float,
-                 attempts: int, precision: str = "mixed", controller: str = "reference"):
+                 attempts: int, precision: str = "mixed", controller: str = "reference",
+                 mlp: GbMlp | None = None):
     logs = []
     for seed in seeds:
         x0 = ic_plummer(n, seed)
         exe = Gb300Executor(precision=precision, controller=controller, attempts_per_sync=16,
-                            log_steps=attempts)
+                            log_steps=attempts, mlp=mlp)
         it = Integrator(tab, NBodyODE(n, softening, 1.0 / n), exe)
         it.start(x0, 0.0, tf, tol, tol)
         it.advance(attempts)
@@ -45,14 +49,16 @@ def collect_logs(seeds, n: int, softening: float, tab: str, tol: float, tf: floa
     return logs
 
 
-def build_dataset(logs, q: int, rho: float = 0.5):
+def build_dataset(logs, q: int, rho: float = 0.6):
     xs, ys = [], []
+    log_safety = np.log(0.38) / (1.0 + q)
     for rec in logs:
         for k in range(len(rec) - 1):
             if rec[k, ACCEPTED] < 0.5:
                 continue
+            base = log_safety - rec[k, LOG_ERR] / (q + 1)
             target = (rec[k + 1, LOG_DT] + (np.log(rho) - rec[k + 1, LOG_ERR]) / (q + 1)
-                      - rec[k, LOG_DT])
+                      - rec[k, LOG_DT] - base)
             if not np.isfinite(target):
                 continue
             xs.append(rec[k, FEAT])
@@ -95,6 +101,26 @@ def train(x: np.ndarray, y: np.ndarray, epochs: int = 3000, lr: float = 3e-3,
                              over_weight, C.byref(loss), None), "gb_mlp_train")
     torch.cuda.synchronize()
     return _from_device_struct(w), float(loss.value)
+
+
+def fit(seeds, n: int, softening: float, tab: str, tol: float, tf: float, attempts: int,
+        rounds: int = 2, rho: float = 0.6, epochs: int = 3000, over_weight: float = 2.0):
+    """Logs of the reference and PI controllers, a first fit, then rounds of
+    logs collected under the learned controller itself (so the data cover the
+    states it visits) and refits.  Returns (network, info)."""
+    q = min(tableau(tab).p, tableau(tab).pt)
+    logs = collect_logs(seeds, n, softening, tab, tol, tf, attempts, controller="reference")
+    logs += collect_logs(seeds, n, softening, tab, tol, tf, attempts, controller="pi")
+    info = []
+    m = None
+    for r in range(max(rounds, 1)):
+        if m is not None:
+            logs += collect_logs(seeds, n, softening, tab, tol, tf, attempts,
+                                 controller="learned", mlp=m)
+        x, y = build_dataset(logs, q, rho)
+        m, loss = train(x, y, epochs=epochs, over_weight=over_weight)
+        info.append({"round": r, "samples": int(len(y)), "loss": loss})
+    return m, info
 
 
 def run_window(n: int, softening: float, tab: str, tol: float, t_end: float, seed: int,

@@ -163,3 +163,36 @@ def test_enqueue_and_state(gb, torch_cuda):
     x, t = it.state()
     assert t == s["t"] and x.shape[0] == 6 * n
     it.close()
+
+
+@pytest.mark.parametrize("tag", ["ball64_dopri5", "ball64_rkf78", "plummer256_rkf78",
+                                 "config1_ball1024_dopri5"])
+def test_exact_mode_reproduces_reference_bits(gb, torch_cuda, tag):
+    """Exact mode: serial partner order, serial norm, IEEE stage sums and a
+    correctly rounded pow in the step-size formulas -- the whole accepted
+    trajectory equals the reference's single-threaded run bit for bit."""
+    path = os.path.join(GOLDEN, f"nbody_{tag}.npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture missing")
+    d = np.load(path)
+    n, soft, mass, t0, tf, tol = d["meta"]
+    n = int(n)
+    times, states, _ = run(gb, str(d["tableau"]), n, soft, mass, d["x0"], t0, tf, tol,
+                           exact=True)
+    np.testing.assert_array_equal(times, d["times"])
+    np.testing.assert_array_equal(states[-1], d["final"])
+    np.testing.assert_array_equal(states[len(states) // 2], d["mid"])
+
+
+def test_sorted_and_unsorted_mixed_paths_agree(gb, torch_cuda):
+    n = 3000
+    x0 = gb.ic_plummer(n, 12)
+    tol = 1e-9
+    t64, s64, _ = run(gb, "RKF78", n, 0.005, 1.0 / n, x0, 0.0, 0.05, tol)
+    ta, sa, _ = run(gb, "RKF78", n, 0.005, 1.0 / n, x0, 0.0, 0.05, tol, precision="mixed",
+                    spatial_sort=True, attempts_per_sync=4)
+    tb, sb, _ = run(gb, "RKF78", n, 0.005, 1.0 / n, x0, 0.0, 0.05, tol, precision="mixed",
+                    spatial_sort=False)
+    assert abs(len(ta) - len(t64)) <= 2 and abs(len(tb) - len(t64)) <= 2
+    assert np.max(np.abs(sa[-1] - s64[-1])) <= 1e-6
+    assert np.max(np.abs(sb[-1] - s64[-1])) <= 1e-6

@@ -140,3 +140,36 @@ def test_energy_kernel_matches_oracle(gb, orc, torch_cuda):
 def test_invalid_mixed_softening_rejected(gb, torch_cuda):
     with pytest.raises(gb.GbError):
         gb.nbody_rhs_mixed(_x(10, 1), 10, 0.0, 0.1)
+
+
+@pytest.mark.parametrize("n,soft,gen", [(1024, 0.01, "ball"), (4096, 0.005, "plummer"),
+                                        (16384, 0.005, "plummer"), (3001, 0.003, "binary"),
+                                        (130, 0.05, "plummer"), (65536, 0.002, "cold")])
+def test_rhs_mixed_sorted_within_1e6_of_fp64(gb, torch_cuda, n, soft, gen):
+    """Morton-sorted tiles with the tile-centroid far path: same bound as the
+    hi/lo path, rows in body order."""
+    x = {"ball": lambda: gb.ic_uniform_ball(n, 1, 0.1), "plummer": lambda: gb.ic_plummer(n, 2),
+         "binary": lambda: gb.ic_binary_plummer(n, 3, 0.1, 1e-3, 1e-2),
+         "cold": lambda: gb.ic_cold_sphere(n, 4, 0.01)}[gen]()
+    ref = gb.nbody_rhs_f64(x, n, soft, 1.0 / n).cpu().numpy()
+    got = gb.nbody_rhs_mixed_sorted(x, n, soft, 1.0 / n).cpu().numpy()
+    np.testing.assert_array_equal(got[: 3 * n], ref[: 3 * n])
+    a_g, a_r = got[3 * n:].reshape(-1, 3), ref[3 * n:].reshape(-1, 3)
+    assert _rel(a_g, a_r) <= 1e-6, _rel(a_g, a_r)
+    per = np.linalg.norm(a_g - a_r, axis=1) / np.linalg.norm(a_r, axis=1)
+    assert np.median(per) <= 1e-6, np.median(per)
+
+
+def test_rhs_mixed_sorted_masses_and_displaced(gb, torch_cuda):
+    n = 2000
+    x = gb.ic_plummer(n, 5)
+    m = np.random.default_rng(2).uniform(0.5, 1.5, n)
+    m /= m.sum()
+    mt = gb.to_device(m)
+    ref = gb.nbody_rhs_f64(x, n, 0.01, masses=mt).cpu().numpy()
+    got = gb.nbody_rhs_mixed_sorted(x, n, 0.01, masses=mt).cpu().numpy()
+    assert _rel(got[3 * n:], ref[3 * n:]) <= 1e-6
+    xs = x.copy()
+    xs[: 3 * n] += 1.0e4
+    got2 = gb.nbody_rhs_mixed_sorted(xs, n, 0.01, masses=mt).cpu().numpy()
+    assert _rel(got2[3 * n:], ref[3 * n:]) <= 2e-6
