@@ -219,7 +219,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--controller", default="reference", choices=["reference", "pi", "learned"])
     ap.add_argument("--mlp", default=None, help="trained proposer weights (learned controller)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c5a", "c5b"],
+    ap.add_argument("--workload", default="c2",
+                    choices=["c2", "c2_f64", "c1", "c3", "c5a", "c5b"],
                     help="c2 (default, the headline), or another configuration")
     args = ap.parse_args()
     world, rank, local = dist_setup()
@@ -405,7 +406,30 @@ def run_other_workload(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     line = {"metric": METRIC, "unit": "accepted steps/s", "n_gpus": 1, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "data": "synthetic", "warmup": args.warmup}
-    if args.workload == "c1":
+    if args.workload == "c2_f64":
+        # the plain FP64 GB300 path over the whole headline trajectory
+        W = WORKLOAD
+        n, eps = W["n_particles"], W["softening"]
+        x0 = gb.to_device(gb.ic_plummer(n, W["seed"], 1.0))
+        it = gb.Integrator(W["tableau"], gb.NBodyODE(n, eps, 1.0 / n),
+                           gb.Gb300Executor(precision="f64", attempts_per_sync=16), stream=stream)
+
+        def job():
+            it.start(x0, W["t0"], W["tf"], W["atol"], W["rtol"])
+            assert it.advance(0) == 0
+            return it.stats()
+        ms, st = _timed(torch, stream, job, 1, flush)
+        e0 = gb.energy(x0, n, eps, 1.0 / n)
+        e1 = gb.energy(it.state()[0], n, eps, 1.0 / n)
+        line.update(value=st[0]["n_accepted"] / (ms / 1e3), dtype="f64", steps=1,
+                    ms_per_step=ms, warmup=0,
+                    pair_interactions_per_s=st[0]["n_rhs"] * n * (n - 1) / (ms / 1e3),
+                    per_step={"accepted": st[0]["n_accepted"], "attempts": st[0]["n_attempts"],
+                              "rhs": st[0]["n_rhs"]},
+                    energy_rel_err=abs(e1["e"] - e0["e"]) / abs(e0["e"]),
+                    config={**W, "precision": "f64", "step": "whole integration"})
+        it.close()
+    elif args.workload == "c1":
         n, eps, tol = 1024, 0.01, 1e-10
         x0 = gb.to_device(gb.ic_uniform_ball(n, 1, 0.1))
         it = gb.Integrator("DOPRI5", gb.NBodyODE(n, eps, 1.0 / n),

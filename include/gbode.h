@@ -346,6 +346,13 @@ int gb_integrator_launch_stage(gb_integrator it, int32_t stage);
 /* Launch geometry chosen for the fused stage kernel (reserved = threads per
  * CTA) and the number of CTAs per launch. */
 int gb_integrator_geometry(gb_integrator it, gb_force_tiling* out, int64_t* n_ctas);
+/* Dense output (DOPRI5 only, the continuous extension of NumericalRecipes/ */
+/* StepperDopr5.hpp:179-219, which the template integrator lacks): states  */
+/* at the given ascending times are evaluated on the device after each     */
+/* accepted step, without shortening any step.  Call between create and    */
+/* start; gb_integrator_dense_output copies those computed so far.         */
+int gb_integrator_set_dense_output(gb_integrator it, const double* times_host, int64_t n_times);
+int gb_integrator_dense_output(gb_integrator it, double* x_host, int64_t capacity, int64_t* count);
 /* Copies up to `capacity` controller log records (opts.log_steps > 0). */
 int gb_integrator_log(gb_integrator it, gb_step_log* host_records, int64_t capacity,
                       int64_t* count);
@@ -408,6 +415,34 @@ int gb_batch_launch_stage(gb_batch b, int32_t stage);
 int gb_batch_autotune(gb_batch b, int32_t reps, gb_batch_tiling* chosen, double* best_ms);
 int gb_batch_geometry(gb_batch b, gb_batch_tiling* out, int64_t* n_units);
 int gb_batch_destroy(gb_batch b);
+
+/* ---------------------------------------------------------------------- */
+/* Fixed-step kick-drift-kick leapfrog on the same force kernels.           */
+/* Replaces ParallelLeapfrogIntegrator::integrate                           */
+/* (src/integrator/leapfrog/LeapfrogParallel.hpp:11-41, kernels :57-73):    */
+/* same update formulas and order; x_dev is advanced in place; `save`       */
+/* receives t0 and every step's state (host copy).                         */
+/* ---------------------------------------------------------------------- */
+int gb_leapfrog_nbody(const gb_nbody_system* sys, double* x_dev, double t0, double tf, double dt,
+                      int32_t precision, const gb_force_tiling* tiling, gb_save_fn save,
+                      void* user, int64_t* n_steps, gb_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Trajectory files in the reference's binary format                        */
+/* (src/demo/nbody_io.hpp:4-22; read by scripts/nbody_io/bin_reader.py):   */
+/* uint64 n_times, uint64 n_var, float64 softening, then per saved state    */
+/* float64 t and n_var float64 values.  Records are written by a background */
+/* thread as they arrive; gb_trajectory_close patches n_times.  Pass        */
+/* gb_trajectory_save with the writer as `user` to the integrator to stream */
+/* every accepted state to disk (the reference keeps them all in memory and */
+/* writes at the end).                                                     */
+/* ---------------------------------------------------------------------- */
+typedef struct gb_trajectory_s* gb_trajectory;
+
+int gb_trajectory_open(const char* path, int64_t n_var, double softening, gb_trajectory* out);
+int gb_trajectory_append(gb_trajectory w, double t, const double* x_host);
+void gb_trajectory_save(void* user, double t, const double* x_host, int64_t n_var);
+int gb_trajectory_close(gb_trajectory w, int64_t* n_times);
 
 /* ---------------------------------------------------------------------- */
 /* Energy and momentum diagnostics (FP64).                                 */

@@ -157,6 +157,9 @@ SIGNATURES = {
     "gb_integrator_destroy": (C.c_int, [_VP]),
     "gb_integrator_log": (C.c_int, [_VP, C.POINTER(GbStepLog), _I64, C.POINTER(C.c_int64)]),
     "gb_integrator_launch_stage": (C.c_int, [_VP, _I32]),
+    "gb_integrator_set_dense_output": (C.c_int, [_VP, C.POINTER(C.c_double), _I64]),
+    "gb_integrator_dense_output": (C.c_int, [_VP, C.POINTER(C.c_double), _I64,
+                                             C.POINTER(C.c_int64)]),
     "gb_integrator_geometry": (C.c_int, [_VP, C.POINTER(GbForceTiling), C.POINTER(C.c_int64)]),
     "gb_integrate_nbody": (C.c_int, [C.POINTER(GbTableau), C.POINTER(GbNBodySystem),
                                      C.POINTER(GbIntegrateOpts), _DP, _D, _D, _DP, _DP, _D, _D,
@@ -175,6 +178,13 @@ SIGNATURES = {
     "gb_batch_autotune": (C.c_int, [_VP, _I32, C.POINTER(GbBatchTiling), C.POINTER(C.c_double)]),
     "gb_batch_geometry": (C.c_int, [_VP, C.POINTER(GbBatchTiling), C.POINTER(C.c_int64)]),
     "gb_batch_destroy": (C.c_int, [_VP]),
+    "gb_leapfrog_nbody": (C.c_int, [C.POINTER(GbNBodySystem), _DP, _D, _D, _D, _I32,
+                                    C.POINTER(GbForceTiling), SAVE_FN, _VP,
+                                    C.POINTER(C.c_int64), _VP]),
+    "gb_trajectory_open": (C.c_int, [C.c_char_p, _I64, _D, C.POINTER(C.c_void_p)]),
+    "gb_trajectory_append": (C.c_int, [_VP, _D, C.POINTER(C.c_double)]),
+    "gb_trajectory_save": (None, [_VP, _D, C.POINTER(C.c_double), _I64]),
+    "gb_trajectory_close": (C.c_int, [_VP, C.POINTER(C.c_int64)]),
     "gb_nbody_energy_workspace_bytes": (C.c_size_t, [_I64]),
     "gb_nbody_energy_f64": (C.c_int, [_DP, _I64, _D, _D, _DP, _VP, C.c_size_t, _DP, _VP]),
     "gb_ic_uniform_ball": (C.c_int, [_I64, C.c_uint64, _D, C.POINTER(C.c_double)]),
@@ -564,6 +574,20 @@ class Integrator:
         arr = np.ctypeslib.as_array(C.cast(recs, C.POINTER(C.c_float)), shape=(max(n, 1), 20))
         return arr[:n].copy()
 
+    def set_dense_output(self, times):
+        self._dense_t = np.ascontiguousarray(times, dtype=np.float64)
+        check(lib().gb_integrator_set_dense_output(
+            self.h, self._dense_t.ctypes.data_as(C.POINTER(C.c_double)), len(self._dense_t)),
+            "gb_integrator_set_dense_output")
+
+    def dense_output(self) -> np.ndarray:
+        cnt = C.c_int64(0)
+        n = len(getattr(self, "_dense_t", []))
+        out = np.zeros((max(n, 1), self.ode.n_var))
+        check(lib().gb_integrator_dense_output(self.h, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                               n, C.byref(cnt)), "gb_integrator_dense_output")
+        return out[: int(cnt.value)]
+
     def launch_stage(self, stage: int):
         check(lib().gb_integrator_launch_stage(self.h, stage), "gb_integrator_launch_stage")
 
@@ -707,6 +731,62 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class ParallelLeapfrogIntegrator:
+    """ParallelLeapfrogIntegrator::integrate(x0, t0, tf, dt, ode, output, exe)
+    (src/integrator/leapfrog/LeapfrogParallel.hpp:11-41) on the device."""
+
+    @staticmethod
+    def integrate(x0, t0: float, tf: float, dt: float, ode: NBodyODE, output,
+                  exe: Gb300Executor):
+        x = to_device(x0).clone()
+        sysd = GbNBodySystem(ode.n_particles, ode.softening, ode.mass,
+                             _ptr(ode.masses) if ode.masses is not None else None)
+        cb = SAVE_FN()
+        if output is not None:
+            def _cb(_u, t, xp, n):
+                output.save_state(t, np.ctypeslib.as_array(xp, shape=(n,)))
+            cb = SAVE_FN(_cb)
+        steps = C.c_int64(0)
+        check(lib().gb_leapfrog_nbody(C.byref(sysd), _ptr(x), t0, tf, dt, PREC[exe.precision],
+                                      C.byref(exe.tile) if exe.tile else None, cb, None,
+                                      C.byref(steps), _stream()), "gb_leapfrog_nbody")
+        return x, int(steps.value)
+
+
+class TrajectoryWriter:
+    """Trajectory file in the reference's binary format (gb_trajectory_*).
+    Usable as an integrator output: ``save_state(t, x)``; or pass
+    ``writer.c_save`` / ``writer.handle`` to the C save callback slot."""
+
+    def __init__(self, path: str, n_var: int, softening: float):
+        h = C.c_void_p()
+        check(lib().gb_trajectory_open(path.encode(), n_var, softening, C.byref(h)),
+              "gb_trajectory_open")
+        self.handle = h
+        self.n_var = n_var
+
+    def save_state(self, t: float, x) -> None:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        check(lib().gb_trajectory_append(self.handle, t, x.ctypes.data_as(C.POINTER(C.c_double))),
+              "gb_trajectory_append")
+
+    def close(self) -> int:
+        n = C.c_int64(0)
+        if self.handle:
+            check(lib().gb_trajectory_close(self.handle, C.byref(n)), "gb_trajectory_close")
+            self.handle = None
+        return int(n.value)
+
+
+def read_trajectory(path: str):
+    """(times, states, softening) of a file in the reference's format."""
+    with open(path, "rb") as f:
+        n_times, n_var = np.frombuffer(f.read(16), dtype="<u8")
+        softening = float(np.frombuffer(f.read(8), dtype="<f8")[0])
+        data = np.frombuffer(f.read(), dtype="<f8").reshape(int(n_times), int(n_var) + 1)
+    return data[:, 0].copy(), data[:, 1:].copy(), softening
 
 
 def exported_symbols() -> list[str]:

@@ -25,7 +25,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "--expt-relaxed-constexpr", f"-I{INCLUDE}", f"-I{CSRC}"]
 SOURCES = ["rk.cu", "nbody.cu", "integrator.cu", "mlp.cu", "batched.cu", "energy.cu", "ic.cu",
-           "noalloc.cu"]
+           "noalloc.cu", "trajectory.cu",
+           "leapfrog.cu"]
 
 
 def nvcc() -> str:

@@ -104,6 +104,9 @@ __device__ inline void finish_attempt(const DevTableau& tab, const CtrlEnv& P, C
     return;
   }
   if (accepted) {
+    // slots of this attempt's first and last stage derivatives (dense output)
+    c.dense_k0 = c.k0slot;
+    c.dense_klast = (c.k0slot == 0) ? tab.n_stages - 1 : 0;
     c.t += dt;
     c.cur = (c.cur + 1) % P.R;
     if (P.times_ring) P.times_ring[c.cur] = c.t;

@@ -16,6 +16,7 @@
 // attempts.  States live in a ring of R slots so that accepting a step is an
 // index change, and accepted states can be streamed out without stalling the
 // device.
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -205,6 +206,47 @@ __global__ void __launch_bounds__(T, 1024 / T)
   if (threadIdx.x == 0) P.partials[ci.itile] = tile_sum;
 }
 
+// Dense output of DOPRI5 (the continuous extension of Dormand & Prince as
+// in Hairer, Norsett & Wanner and NumericalRecipes/StepperDopr5.hpp:179-219):
+// for each output time in the step just accepted, theta = (t_out - t_old)/h
+// and x(theta) = r1 + theta (r2 + (1-theta) (r3 + theta (r4 + (1-theta) r5)))
+// with r1 = y0, r2 = y1 - y0, r3 = h k1 - r2, r4 = r2 - h k7 - r3,
+// r5 = h (d1 k1 + d3 k3 + d4 k4 + d5 k5 + d6 k6 + d7 k7).
+__global__ void dense_kernel(const __grid_constant__ FusedParams P) {
+  const Ctrl* C = P.ctrl;
+  const long long lo = C->dense_lo, hi = C->dense_hi;
+  if (hi <= lo) return;
+  const long long nv = P.n_var;
+  const int R = P.R;
+  const double* y1 = P.ring + (long long)C->cur * nv;
+  const double* y0 = P.ring + (long long)((C->cur + R - 1) % R) * nv;
+  const double h = C->dt_hist[0];
+  const double t_old = C->t - h;
+  const double* k1 = P.ks + (long long)C->dense_k0 * nv;
+  const double* k7 = P.ks + (long long)C->dense_klast * nv;
+  const double* k3 = P.ks + 2 * nv;
+  const double* k4 = P.ks + 3 * nv;
+  const double* k5 = P.ks + 4 * nv;
+  const double* k6 = P.ks + 5 * nv;
+  const double d1 = -12715105075.0 / 11282082432.0, d3 = 87487479700.0 / 32700410799.0,
+               d4 = -10690763975.0 / 1880347072.0, d5 = 701980252875.0 / 199316789632.0,
+               d6 = -1453857185.0 / 822651844.0, d7 = 69997945.0 / 29380423.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double r1 = y0[i];
+    const double r2 = y1[i] - y0[i];
+    const double r3 = h * k1[i] - r2;
+    const double r4 = r2 - h * k7[i] - r3;
+    const double r5 =
+        h * (d1 * k1[i] + d3 * k3[i] + d4 * k4[i] + d5 * k5[i] + d6 * k6[i] + d7 * k7[i]);
+    for (long long j = lo; j < hi; ++j) {
+      const double th = (P.dense_t[j] - t_old) / h;
+      const double s1 = 1.0 - th;
+      P.dense_out[j * nv + i] = r1 + th * (r2 + s1 * (r3 + th * (r4 + s1 * r5)));
+    }
+  }
+}
+
 // End of an attempt: one CTA reduces the per-tile partial sums in tile
 // order (or, in exact mode, the per-element squares in element order, as the
 // reference's serial executor adds them), forms err = sqrt(sum / n_var)
@@ -270,6 +312,13 @@ __global__ void __launch_bounds__(256)
     if (k0_valid) c.n_rhs_saved += 1;
     const CtrlEnv env{P.log, P.log_capacity, P.times_ring, P.R, P.n};
     finish_attempt(tab, env, c, err, sh_flag ? (double)outv : 0.0, sh_flag != 0);
+    c.dense_lo = c.dense_hi = c.dense_next;
+    if (P.dense_t && c.last_accepted) {
+      long long j = c.dense_next;
+      while (j < P.n_dense && P.dense_t[j] <= c.t) ++j;
+      c.dense_hi = j;
+      c.dense_next = j;
+    }
     *C = c;
   }
 }
@@ -516,9 +565,14 @@ struct gb_integrator_s {
   float4* PYF = nullptr;
   gb::TileMeta* MX = nullptr;
   gb::TileMeta* MY = nullptr;
+  double* dense_t = nullptr;
+  double* dense_out = nullptr;
+  long long n_dense = 0;
   void* mlp_dev = nullptr;
   // host
   gb::Ctrl* hctrl = nullptr;  // pinned
+  double* hstage = nullptr;   // pinned R * n_var (recording)
+  double* htimes = nullptr;   // pinned R
   std::vector<double> hstate;
   long long delivered = 0;    // accepted states handed to the save callback
   bool started = false;
@@ -552,10 +606,12 @@ void free_all(gb_integrator_s* it) {
                   it->PY,    it->atol, it->rtol,       it->cref,   it->partials, it->aux,
                   it->sq,    it->dscal, it->norm_work, it->masses, it->log,      it->mlp_dev,
                   it->perm,  it->vals, it->keys,     it->keys_alt, it->cub_temp, it->bbox,
-                  it->PXF,   it->PYF,  it->MX,       it->MY};
+                  it->PXF,   it->PYF,  it->MX,       it->MY,       it->dense_t, it->dense_out};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (it->hctrl) cudaFreeHost(it->hctrl);
+  if (it->hstage) cudaFreeHost(it->hstage);
+  if (it->htimes) cudaFreeHost(it->htimes);
   if (it->ev) cudaEventDestroy(it->ev);
   if (it->stream && it->own_stream) cudaStreamDestroy(it->stream);
 }
@@ -566,6 +622,11 @@ int launch_fused(gb_integrator_s* it, int s) {
   if (s == it->S - 1) {
     control_kernel<<<1, 256, 0, it->stream>>>(it->tab, it->params);
     GB_CUDA_TRY(cudaGetLastError());
+    if (it->params.dense_t) {
+      dense_kernel<<<(unsigned)std::min<long long>((it->n_var + 255) / 256, 1024), 256, 0,
+                     it->stream>>>(it->params);
+      GB_CUDA_TRY(cudaGetLastError());
+    }
   }
   return GB_OK;
 }
@@ -610,22 +671,27 @@ int read_ctrl(gb_integrator_s* it) {
 }
 
 // Hands newly accepted states to the callback, in order (ring slots
-// delivered+1 .. n_accepted).
+// delivered+1 .. n_accepted): each contiguous run of slots is copied to
+// pinned staging in one transfer, then delivered state by state.
 int drain(gb_integrator_s* it, gb_save_fn save, void* user) {
   if (!save || !it->opts.record) {
     it->delivered = it->hctrl->n_accepted;
     return GB_OK;
   }
   const long long upto = it->hctrl->n_accepted;
-  for (long long k = it->delivered + 1; k <= upto; ++k) {
-    const int slot = (int)(k % it->R);
-    double t = 0.0;
-    GB_CUDA_TRY(cudaMemcpyAsync(&t, it->times_ring + slot, sizeof(double),
+  long long k = it->delivered + 1;
+  while (k <= upto) {
+    const int slot0 = (int)(k % it->R);
+    const long long run = std::min<long long>(upto - k + 1, it->R - slot0);
+    GB_CUDA_TRY(cudaMemcpyAsync(it->hstage, it->ring + (long long)slot0 * it->n_var,
+                                (size_t)run * it->n_var * sizeof(double),
                                 cudaMemcpyDeviceToHost, it->stream));
-    GB_CUDA_TRY(cudaMemcpyAsync(it->hstate.data(), it->ring + (long long)slot * it->n_var,
-                                it->n_var * sizeof(double), cudaMemcpyDeviceToHost, it->stream));
+    GB_CUDA_TRY(cudaMemcpyAsync(it->htimes, it->times_ring + slot0, (size_t)run * sizeof(double),
+                                cudaMemcpyDeviceToHost, it->stream));
     GB_CUDA_TRY(cudaStreamSynchronize(it->stream));
-    save(user, t, it->hstate.data(), it->n_var);
+    for (long long j = 0; j < run; ++j)
+      save(user, it->htimes[j], it->hstage + j * it->n_var, it->n_var);
+    k += run;
   }
   it->delivered = upto;
   return GB_OK;
@@ -747,6 +813,10 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   }
 #undef GB_ALLOC
   e = cudaMallocHost((void**)&it->hctrl, sizeof(Ctrl));
+  if (e == cudaSuccess && opts.record)
+    e = cudaMallocHost((void**)&it->hstage, (size_t)it->R * nv * sizeof(double));
+  if (e == cudaSuccess && opts.record)
+    e = cudaMallocHost((void**)&it->htimes, (size_t)it->R * sizeof(double));
   if (e == cudaSuccess) {
     // Graphs cannot be captured on the legacy default stream: run on the
     // caller's stream when it is a real stream, else on an owned one.
@@ -923,6 +993,56 @@ extern "C" int gb_integrator_advance(gb_integrator it, int64_t max_attempts, gb_
   GB_CUDA_TRY(cudaEventRecord(it->ev, it->stream));
   GB_CUDA_TRY(cudaStreamWaitEvent(it->user_stream, it->ev, 0));
   return it->hctrl->status;
+}
+
+// Output at the given times (ascending, within (t0, tf]) by the DOPRI5 dense
+// formula after every accepted step.  Call after create and before start;
+// the graph is rebuilt.
+extern "C" int gb_integrator_set_dense_output(gb_integrator it, const double* times_host,
+                                              int64_t n_times) {
+  if (!it || n_times < 0 || (n_times > 0 && !times_host)) return GB_ERR_INVALID_ARGUMENT;
+  gb_tableau dp;
+  gb_tableau_builtin(GB_DOPRI5, &dp);
+  if (std::memcmp(&dp, &it->htab, sizeof dp) != 0) return GB_ERR_UNSUPPORTED;
+  for (int64_t j = 1; j < n_times; ++j)
+    if (!(times_host[j] >= times_host[j - 1])) return GB_ERR_INVALID_ARGUMENT;
+  if (it->dense_t) cudaFree(it->dense_t);
+  if (it->dense_out) cudaFree(it->dense_out);
+  it->dense_t = nullptr;
+  it->dense_out = nullptr;
+  it->n_dense = n_times;
+  if (n_times > 0) {
+    GB_CUDA_TRY(cudaMalloc((void**)&it->dense_t, n_times * sizeof(double)));
+    GB_CUDA_TRY(cudaMalloc((void**)&it->dense_out, (size_t)n_times * it->n_var * sizeof(double)));
+    GB_CUDA_TRY(cudaMemcpy(it->dense_t, times_host, n_times * sizeof(double),
+                           cudaMemcpyHostToDevice));
+  }
+  it->params.dense_t = it->dense_t;
+  it->params.dense_out = it->dense_out;
+  it->params.n_dense = n_times;
+  if (it->exec) {
+    cudaGraphExecDestroy(it->exec);
+    cudaGraphDestroy(it->graph);
+    it->exec = nullptr;
+    it->graph = nullptr;
+  }
+  return GB_OK;
+}
+
+// Copies the dense outputs computed so far (count = outputs whose time has
+// been passed) to x_host [count][n_var].
+extern "C" int gb_integrator_dense_output(gb_integrator it, double* x_host, int64_t capacity,
+                                          int64_t* count) {
+  if (!it || !count) return GB_ERR_INVALID_ARGUMENT;
+  GB_TRY(read_ctrl(it));
+  const long long c = std::min<long long>(it->hctrl->dense_next, it->n_dense);
+  *count = c;
+  if (x_host && capacity > 0 && c > 0) {
+    const long long m = std::min<long long>(c, capacity);
+    GB_CUDA_TRY(cudaMemcpy(x_host, it->dense_out, (size_t)m * it->n_var * sizeof(double),
+                           cudaMemcpyDeviceToHost));
+  }
+  return GB_OK;
 }
 
 extern "C" int gb_integrator_launch_stage(gb_integrator it, int32_t stage) {

@@ -37,6 +37,10 @@ struct Ctrl {
   int last_accepted;
   int learned_active; // the current attempt uses a learned proposal
   int exact_pow;      // step-size formulas with the correctly rounded pow
+  // dense output (DOPRI5): output times [dense_lo, dense_hi) fall in the
+  // step just accepted; its first / last stage derivatives are in these slots
+  long long dense_next, dense_lo, dense_hi;
+  int dense_k0, dense_klast;
   unsigned ticket;
   unsigned ticket2;
 };
@@ -82,6 +86,10 @@ struct FusedParams {
   float4* PYF;           // 2 * n far records (stage states)
   TileMeta* MX;          // 2 * n_itiles tile metadata (x0 / x_new)
   TileMeta* MY;          // 2 * n_itiles (stage states)
+  // dense output
+  const double* dense_t; // n_dense output times (ascending), or null
+  long long n_dense;
+  double* dense_out;     // n_dense * n_var
 };
 
 }  // namespace gb

@@ -196,3 +196,35 @@ def test_sorted_and_unsorted_mixed_paths_agree(gb, torch_cuda):
     assert abs(len(ta) - len(t64)) <= 2 and abs(len(tb) - len(t64)) <= 2
     assert np.max(np.abs(sa[-1] - s64[-1])) <= 1e-6
     assert np.max(np.abs(sb[-1] - s64[-1])) <= 1e-6
+
+
+def test_dopri5_dense_output(gb, torch_cuda):
+    """Dense output between steps (DOPRI5 continuous extension): states at the
+    requested times agree with integrations stopped exactly there, and at a
+    step's own end time with that step's state."""
+    n, soft, tol, tf = 64, 0.05, 1e-9, 0.3
+    x0 = gb.ic_plummer(n, 21)
+    ode = gb.NBodyODE(n, soft, 1.0 / n)
+    out = gb.RawOutput()
+    it = gb.Integrator("DOPRI5", ode, gb.Gb300Executor(attempts_per_sync=4), record=True)
+    probe = gb.RawOutput()
+    gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, tf, tol, tol, ode, probe,
+                                              gb.Gb300Executor())
+    step_t = np.array(probe.times())
+    times = np.sort(np.concatenate([np.linspace(0.013, 0.29, 17), step_t[3:6]]))
+    it.set_dense_output(times)
+    it.start(x0, 0.0, tf, tol, tol, out)
+    assert it.advance(0, out) == 0
+    dense = it.dense_output()
+    it.close()
+    assert dense.shape == (len(times), 6 * n)
+    for j, t in enumerate(times):
+        ref = gb.RawOutput()
+        gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, t, 1e-12, 1e-12, ode, ref,
+                                                  gb.Gb300Executor())
+        assert np.max(np.abs(dense[j] - ref.states()[-1])) <= 100 * tol, t
+    states = np.array(out.states())
+    for t in step_t[3:6]:
+        k = int(np.where(np.array(out.times()) == t)[0][0])
+        j = int(np.where(times == t)[0][0])
+        np.testing.assert_allclose(dense[j], states[k], rtol=0, atol=1e-13)

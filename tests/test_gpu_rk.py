@@ -99,3 +99,24 @@ def test_fixed_step_trajectory(gb, orc, torch_cuda, name, tile):
         np.testing.assert_array_equal(got, ref)
     else:
         assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) <= 1e-12
+
+
+@pytest.mark.parametrize("tile,exact", [((1, 1, 0), True), ((0, 0, 0), False)])
+def test_leapfrog_matches_oracle(gb, orc, torch_cuda, tile, exact):
+    """ParallelLeapfrogIntegrator (LeapfrogParallel.hpp:11-41): bit-identical
+    with the serial tiling, <= 1e-12 otherwise."""
+    n, soft, dt = 200, 0.02, 1e-3
+    x0 = gb.ic_plummer(n, 17)
+    ode, _ = orc.nbody_ode(n, soft, 1.0 / n)
+    ref, steps_ref = orc.leapfrog(ode, x0, 0.0, 0.05, dt)
+    out = gb.RawOutput()
+    exe = gb.Gb300Executor(tile=gb.tiling(*tile))
+    x, steps = gb.ParallelLeapfrogIntegrator.integrate(x0, 0.0, 0.05, dt,
+                                                       gb.NBodyODE(n, soft, 1.0 / n), out, exe)
+    assert steps == steps_ref and len(out.times()) == steps + 1
+    got = x.cpu().numpy()
+    if exact:
+        np.testing.assert_array_equal(got, ref)
+    else:
+        assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) <= 1e-12
+    np.testing.assert_array_equal(np.array(out.states()[-1]), got)
