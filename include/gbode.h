@@ -106,7 +106,8 @@ typedef struct {
   int32_t j_split;       /* CTAs per thread-block cluster sharing one i-tile: 1,2,4,8 (0 = auto) */
   int32_t lanes;         /* lanes per body inside a warp: 1,2,4,8 (0 = auto) */
   int32_t bodies_per_cta;/* i-bodies per CTA: 32..256 (0 = auto) */
-  int32_t reserved;
+  int32_t reserved;      /* mixed precision: 1 = scalar FP32 path instead of the packed
+                            f32x2 path (two bodies per thread, uniform masses) */
 } gb_force_tiling;
 
 int gb_nbody_rhs_f64(const double* x_dev, double* dxdt_dev, int64_t n_particles,
@@ -292,8 +293,8 @@ typedef struct {
   gb_force_tiling tiling;     /* 0 fields = auto */
   const void* mlp;            /* gb_mlp* weights for GB_CTRL_LEARNED (device-resident copy made) */
   int32_t log_steps;          /* record per-attempt controller logs on the device */
-  int32_t spatial_sort;       /* mixed precision: Morton-sorted tiles with the far-field
-                                 path (0 = on, -1 = off) */
+  int32_t spatial_sort;       /* mixed precision: 1 = Morton-sorted tiles with the
+                                 far-field path (pays off for large N), 0 = off */
 } gb_integrate_opts;
 
 typedef struct {

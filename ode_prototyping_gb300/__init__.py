@@ -91,7 +91,7 @@ class GbBatchOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("controller", C.c_int32), ("fsal", C.c_int32),
                 ("attempts_per_sync", C.c_int32), ("max_attempts", C.c_int64),
                 ("host_wait_timeout_s", C.c_double), ("pi_beta", C.c_double),
-                ("tiling", GbBatchTiling)]
+                ("tiling", GbBatchTiling), ("mlp", C.c_void_p)]
 
 
 class GbStepLog(C.Structure):
@@ -260,8 +260,9 @@ def tableau(name_or_struct) -> GbTableau:
     return t
 
 
-def tiling(j_split=0, lanes=0, bodies_per_cta=0) -> GbForceTiling:
-    return GbForceTiling(j_split, lanes, bodies_per_cta, 0)
+def tiling(j_split=0, lanes=0, bodies_per_cta=0, scalar=False) -> GbForceTiling:
+    """Force-kernel tiling; scalar=True selects the scalar FP32 mixed path."""
+    return GbForceTiling(j_split, lanes, bodies_per_cta, 1 if scalar else 0)
 
 
 # ----------------------------------------------------------------------------
@@ -461,7 +462,7 @@ class Gb300Executor:
     pi_beta: float = 0.04
     mlp: GbMlp | None = None
     log_steps: int = 0
-    spatial_sort: bool = True
+    spatial_sort: bool = False
 
     def rhs(self, ode: NBodyODE, x, dxdt):
         if self.precision == "f64":
@@ -488,7 +489,7 @@ class Gb300Executor:
             self._mlp_keep = self.mlp
             o.mlp = C.cast(C.pointer(self.mlp), C.c_void_p)
         o.log_steps = self.log_steps
-        o.spatial_sort = 0 if self.spatial_sort else -1
+        o.spatial_sort = 1 if self.spatial_sort else 0
         return o
 
 
@@ -641,7 +642,7 @@ class Batch:
 
     def __init__(self, tab, n_particles, softening, mass=None, precision="f64",
                  controller="reference", attempts_per_sync=8, fsal=True, max_attempts=0,
-                 tiling: GbBatchTiling | None = None, stream=None):
+                 tiling: GbBatchTiling | None = None, stream=None, mlp: GbMlp | None = None):
         self.tab = tableau(tab)
         self.n = np.ascontiguousarray(n_particles, dtype=np.int64)
         self.ns = len(self.n)
@@ -658,6 +659,9 @@ class Batch:
         o.host_wait_timeout_s = 600.0
         if tiling is not None:
             o.tiling = tiling
+        if mlp is not None:
+            self._mlp_keep = mlp
+            o.mlp = C.cast(C.pointer(mlp), C.c_void_p)
         self.opts = o
         h = C.c_void_p()
         check(lib().gb_batch_create(C.byref(self.tab), self.ns,

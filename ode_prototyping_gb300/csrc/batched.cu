@@ -71,6 +71,7 @@ struct BatchParams {
   double* aux;           // per unit
   unsigned* n_done;
   long long total_var, total_bodies;
+  const void* mlp;       // learned proposer (device copy) or null
 };
 
 template <int PREC, int T, int L, int BPT>
@@ -154,10 +155,11 @@ __global__ void __launch_bounds__(T)
 }
 
 // One warp per system: ordered reduction of its tile partials, then the
-// controller (lane 0).
+// controller (lane 0); a learned proposal is evaluated by the whole warp.
 __global__ void __launch_bounds__(128)
     batch_control_kernel(const __grid_constant__ DevTableau tab,
                          const __grid_constant__ BatchParams P) {
+  __shared__ float feat[4][kIn];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int k = blockIdx.x * 4 + warp;
   if (k >= P.n_sys) return;
@@ -176,15 +178,28 @@ __global__ void __launch_bounds__(128)
     v = dadd(v, __shfl_xor_sync(0xffffffffu, v, off));
     m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
   }
+  const double err = sqrt(v / (double)(6 * sy.n));
+  int want = 0;
+  if (lane == 0) {
+    Ctrl pre = *C;
+    if (!pre.k0_valid) pre.max_abs_acc = m;
+    want = P.mlp && pre.controller == GB_CTRL_LEARNED && isfinite(err) && err <= 1.0;
+    if (want) {
+      preview_history(pre, err, true);
+      make_features(pre, tab, sy.n, feat[warp]);
+    }
+  }
+  want = __shfl_sync(0xffffffffu, want, 0);
+  __syncwarp();
+  const float learned = want ? mlp_infer_warp(P.mlp, feat[warp]) : 0.f;
   if (lane == 0) {
     Ctrl c = *C;
     const int k0_valid = c.k0_valid;
     if (!k0_valid) c.max_abs_acc = m;
     c.n_rhs += k0_valid ? S - 1 : S;
     if (k0_valid) c.n_rhs_saved += 1;
-    const double err = sqrt(v / (double)(6 * sy.n));
     const CtrlEnv env{nullptr, 0, nullptr, 2, sy.n};
-    finish_attempt(tab, env, c, err, 0.0, false);
+    finish_attempt(tab, env, c, err, (double)learned, want != 0);
     *C = c;
     if (c.done) atomicAdd(P.n_done, 1u);
   }
@@ -399,6 +414,7 @@ struct gb_batch_s {
          *aux = nullptr, *dscal = nullptr, *tv = nullptr;
   gb::PackedBody *PX = nullptr, *PY = nullptr;
   unsigned* n_done = nullptr;
+  void* mlp_dev = nullptr;
   gb::Ctrl* hctrl = nullptr;
   unsigned* hdone = nullptr;
   cudaStream_t stream = nullptr;
@@ -554,7 +570,7 @@ void free_batch(gb_batch_s* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   void* bufs[] = {b->sys,  b->units, b->sys_units, b->body_sys, b->ctrl, b->ring, b->ks,
                   b->Y,    b->cref,  b->partials,  b->aux,      b->dscal, b->tv,  b->PX,
-                  b->PY,   b->n_done};
+                  b->PY,   b->n_done, b->mlp_dev};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (b->hctrl) cudaFreeHost(b->hctrl);
@@ -580,8 +596,9 @@ extern "C" int gb_batch_create(const gb_tableau* tab, int32_t n_sys, const int64
   if (opts_in) opts = *opts_in;
   if (opts.precision != GB_PREC_F64 && opts.precision != GB_PREC_MIXED)
     return GB_ERR_INVALID_ARGUMENT;
-  if (opts.controller != GB_CTRL_REFERENCE && opts.controller != GB_CTRL_PI)
-    return GB_ERR_UNSUPPORTED;
+  if (opts.controller < GB_CTRL_REFERENCE || opts.controller > GB_CTRL_LEARNED)
+    return GB_ERR_INVALID_ARGUMENT;
+  if (opts.controller == GB_CTRL_LEARNED && !opts.mlp) return GB_ERR_INVALID_ARGUMENT;
   if (opts.attempts_per_sync <= 0) opts.attempts_per_sync = 8;
   if (opts.host_wait_timeout_s <= 0.0) opts.host_wait_timeout_s = 600.0;
   if (opts.pi_beta <= 0.0) opts.pi_beta = 0.04;
@@ -673,6 +690,12 @@ extern "C" int gb_batch_create(const gb_tableau* tab, int32_t n_sys, const int64
   P.n_done = b->n_done;
   P.total_var = tv;
   P.total_bodies = tb;
+  if (opts.controller == GB_CTRL_LEARNED) {
+    int mrc = GB_OK;
+    b->mlp_dev = mlp_upload(opts.mlp, &mrc);
+    if (!b->mlp_dev) return fail(mrc == GB_OK ? GB_ERR_INVALID_ARGUMENT : mrc);
+    P.mlp = b->mlp_dev;
+  }
   const int T = opts.tiling.threads_per_cta > 0 ? opts.tiling.threads_per_cta : 128;
   const int L = opts.tiling.lanes > 0 ? opts.tiling.lanes : 2;
   const int BPT = opts.precision == GB_PREC_F64

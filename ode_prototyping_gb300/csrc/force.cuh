@@ -244,6 +244,137 @@ __device__ __forceinline__ void force_mixed_cta(const PackedBody* __restrict__ p
 }
 
 // ---------------------------------------------------------------------------
+// Packed form of force_mixed_cta for two bodies per thread and uniform
+// masses: Blackwell's f32x2 instructions (add/sub/mul/fma on a pair of FP32
+// values) carry both bodies through one instruction stream.  The j-tile is
+// staged in shared memory with every coordinate duplicated into a pair,
+// (hx,hx,hy,hy) (hz,hz,lx,lx) (ly,ly,lz,lz), so each pair operand is one
+// 64-bit register read by a vector load.  Same arithmetic per body as the
+// scalar path (the two lanes of a pair are independent IEEE operations).
+// ---------------------------------------------------------------------------
+typedef unsigned long long f2_t;
+
+__device__ __forceinline__ f2_t f2_pack(float a, float b) {
+  f2_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2_t r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b) {
+  f2_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
+  f2_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+  f2_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
+  f2_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// Staged j-record: three 16-byte pairs-of-pairs (48 bytes per body).
+struct __align__(16) PairRec {
+  ulonglong2 xy;  // (hx,hx), (hy,hy)
+  ulonglong2 zl;  // (hz,hz), (lx,lx)
+  ulonglong2 yz;  // (ly,ly), (lz,lz)
+};
+
+template <int T, int L>
+__device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict__ packed,
+                                                   long long n, long long i0, long long jb,
+                                                   long long je, float eps2, PairRec* sh,
+                                                   double (*part)[3]) {
+  constexpr int BG = T / L;
+  const int g = threadIdx.x / L;
+  const int l = threadIdx.x % L;
+  PackedBody pb[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const long long i = i0 + (long long)q * BG + g;
+    if (i < n) {
+      pb[q] = packed[i];
+    } else {
+      pb[q].hw = make_float4(0.f, 0.f, 0.f, 0.f);
+      pb[q].lo = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  const f2_t HX = f2_pack(pb[0].hw.x, pb[1].hw.x), HY = f2_pack(pb[0].hw.y, pb[1].hw.y),
+             HZ = f2_pack(pb[0].hw.z, pb[1].hw.z);
+  const f2_t LX = f2_pack(pb[0].lo.x, pb[1].lo.x), LY = f2_pack(pb[0].lo.y, pb[1].lo.y),
+             LZ = f2_pack(pb[0].lo.z, pb[1].lo.z);
+  const f2_t E2 = f2_pack(eps2, eps2);
+  float sx[2] = {0.f, 0.f}, sy[2] = {0.f, 0.f}, sz[2] = {0.f, 0.f};
+  float cx[2] = {0.f, 0.f}, cy[2] = {0.f, 0.f}, cz[2] = {0.f, 0.f};
+  constexpr int JT = T;
+  for (long long j0 = jb; j0 < je; j0 += JT) {
+    const int cnt = (int)min((long long)JT, je - j0);
+    __syncthreads();
+    for (int k = threadIdx.x; k < cnt; k += T) {
+      const PackedBody b = packed[j0 + k];
+      PairRec r;
+      r.xy = make_ulonglong2(f2_pack(b.hw.x, b.hw.x), f2_pack(b.hw.y, b.hw.y));
+      r.zl = make_ulonglong2(f2_pack(b.hw.z, b.hw.z), f2_pack(b.lo.x, b.lo.x));
+      r.yz = make_ulonglong2(f2_pack(b.lo.y, b.lo.y), f2_pack(b.lo.z, b.lo.z));
+      sh[k] = r;
+    }
+    __syncthreads();
+    f2_t TX = 0ULL, TY = 0ULL, TZ = 0ULL;  // bit pattern of (+0.f, +0.f)
+#pragma unroll 4
+    for (int jj = l; jj < cnt; jj += L) {
+      const ulonglong2 xy = sh[jj].xy;
+      const ulonglong2 zl = sh[jj].zl;
+      const ulonglong2 yz = sh[jj].yz;
+      const f2_t dx = f2_add(f2_sub(xy.x, HX), f2_sub(zl.y, LX));
+      const f2_t dy = f2_add(f2_sub(xy.y, HY), f2_sub(yz.x, LY));
+      const f2_t dz = f2_add(f2_sub(zl.x, HZ), f2_sub(yz.y, LZ));
+      const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+      float ra, rb;
+      f2_unpack(r2, ra, rb);
+      const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+      const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+      TX = f2_fma(sc, dx, TX);
+      TY = f2_fma(sc, dy, TY);
+      TZ = f2_fma(sc, dz, TZ);
+    }
+    float tx[2], ty[2], tz[2];
+    f2_unpack(TX, tx[0], tx[1]);
+    f2_unpack(TY, ty[0], ty[1]);
+    f2_unpack(TZ, tz[0], tz[1]);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      kahan_add(sx[q], cx[q], tx[q]);
+      kahan_add(sy[q], cy[q], ty[q]);
+      kahan_add(sz[q], cz[q], tz[q]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    double ax = dsub((double)sx[q], (double)cx[q]);
+    double ay = dsub((double)sy[q], (double)cy[q]);
+    double az = dsub((double)sz[q], (double)cz[q]);
+    ax = lane_reduce<L>(ax);
+    ay = lane_reduce<L>(ay);
+    az = lane_reduce<L>(az);
+    if (l == 0) {
+      part[q * BG + g][0] = ax;
+      part[q * BG + g][1] = ay;
+      part[q * BG + g][2] = az;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Mixed precision on spatially sorted bodies.  Bodies are processed in a
 // Morton order, so consecutive 128-body tiles are compact.  Each j-tile J
 // carries its centroid c_J (hi/lo FP32 parts of c_J - c) and radius R_J, and

@@ -35,12 +35,14 @@ size_t norm_workspace_bytes(long long n);
 
 namespace {
 
-template <int PREC, int T, int L, int BPT>
+template <int PREC, int T, int L, int BPT, bool PACKED = false>
 __global__ void __launch_bounds__(T)
     fused_stage_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ FusedParams P, int s) {
   constexpr int BI = (T / L) * BPT;
-  constexpr int SMEM_BODY_BYTES = PREC == GB_PREC_F64 ? 32 * T : (int)sizeof(PackedBody) * T;
+  constexpr int SMEM_BODY_BYTES =
+      PREC == GB_PREC_F64 ? 32 * T
+                          : (PACKED ? (int)sizeof(PairRec) : (int)sizeof(PackedBody)) * T;
   __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
   __shared__ double part[BI][3];
   __shared__ double red[T];
@@ -67,12 +69,16 @@ __global__ void __launch_bounds__(T)
       force_f64_cta<T, L>(ysrc, n, i0, jb, je, P.eps2, P.masses, sh_pos, sh_m, part);
     } else {
       const PackedBody* src = (s == 0) ? P.PX + (long long)px * n : P.PY + (long long)(s & 1) * n;
-      if (P.masses)
+      if constexpr (PACKED) {
+        force_mixed_cta_x2<T, L>(src, n, i0, jb, je, P.eps2f,
+                                 reinterpret_cast<PairRec*>(sh_raw), part);
+      } else if (P.masses) {
         force_mixed_cta<T, L, BPT, false>(src, n, i0, jb, je, P.eps2f,
                                           reinterpret_cast<PackedBody*>(sh_raw), part);
-      else
+      } else {
         force_mixed_cta<T, L, BPT, true>(src, n, i0, jb, je, P.eps2f,
                                          reinterpret_cast<PackedBody*>(sh_raw), part);
+      }
     }
     cluster_combine<BI>(part, ci.rank, ci.size);
   }
@@ -470,7 +476,22 @@ const void* pick_L(int L) {
   }
 }
 
-const void* pick_fused(int prec, int T, int L, int BPT) {
+template <int T>
+const void* pick_packed(int L) {
+  switch (L) {
+    case 1: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 1, 2, true>;
+    case 2: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 2, 2, true>;
+    case 4: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 4, 2, true>;
+    default: return nullptr;
+  }
+}
+
+const void* pick_fused(int prec, int T, int L, int BPT, bool packed = false) {
+  if (prec == GB_PREC_MIXED && packed && BPT == 2) {
+    if (T == 128) return pick_packed<128>(L);
+    if (T == 256) return pick_packed<256>(L);
+    return nullptr;
+  }
   if (prec == GB_PREC_F64) {
     if (BPT != 1) return nullptr;
     switch (T) {
@@ -742,14 +763,15 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   if (opts.precision == GB_PREC_F64) it->geom.BPT = 1;
   if (opts.precision == GB_PREC_MIXED && it->geom.T < 128) it->geom.T = 128;
   // spatially sorted tiles (mixed precision): on unless switched off
-  it->sorted = opts.precision == GB_PREC_MIXED && opts.spatial_sort >= 0;
+  it->sorted = opts.precision == GB_PREC_MIXED && opts.spatial_sort > 0;
   if (it->sorted) {
     if (it->geom.L > 2) it->geom.L = 2;
     it->geom.BPT = it->geom.L;  // i-tile = j-tile = T bodies
   }
   it->geom.n_itiles = (it->n + it->geom.bodies_per_cta() - 1) / it->geom.bodies_per_cta();
   it->kernel = it->sorted ? pick_sorted(it->geom.T, it->geom.L, sys->masses_dev == nullptr)
-                          : pick_fused(opts.precision, it->geom.T, it->geom.L, it->geom.BPT);
+                          : pick_fused(opts.precision, it->geom.T, it->geom.L, it->geom.BPT,
+                                       sys->masses_dev == nullptr && opts.tiling.reserved != 1);
   int rc = GB_OK;
   auto fail = [&](int code) {
     free_all(it);

@@ -115,6 +115,40 @@ __device__ __forceinline__ void mlp_infer_block(const void* mlp_v, const float* 
   __syncthreads();
 }
 
+// Warp-cooperative forward pass (one warp, lane u owns hidden units u and
+// u + 32); the hidden activations move between lanes by shuffles.  All 32
+// lanes must call it; returns the network output on every lane.
+__device__ __forceinline__ float mlp_infer_warp(const void* mlp_v, const float* feat) {
+  const MlpDev* M = reinterpret_cast<const MlpDev*>(mlp_v);
+  const int lane = threadIdx.x & 31;
+  float x[kIn];
+#pragma unroll
+  for (int k = 0; k < kIn; ++k) x[k] = (feat[k] - M->in_mean[k]) * M->in_scale[k];
+  float h1[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int u = lane + 32 * r;
+    float acc = M->b1[u];
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) acc = fmaf(__bfloat162float(M->w1[u * kIn + k]), x[k], acc);
+    h1[r] = silu(acc);
+  }
+  float contrib = 0.f;
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int u = lane + 32 * r;
+    float acc = M->b2[u];
+    for (int k = 0; k < kHid; ++k) {
+      const float hk = __shfl_sync(0xffffffffu, k < 32 ? h1[0] : h1[1], k & 31);
+      acc = fmaf(__bfloat162float(M->w2[u * kHid + k]), hk, acc);
+    }
+    contrib = fmaf(__bfloat162float(M->w3[u]), silu(acc), contrib);
+  }
+#pragma unroll
+  for (int off = 16; off >= 1; off /= 2) contrib += __shfl_xor_sync(0xffffffffu, contrib, off);
+  return M->out_scale * (M->b3 + contrib) + M->out_bias;
+}
+
 // Allocates the device inference copy of a host gb_mlp (rounded to BF16).
 void* mlp_upload(const void* host_mlp, int* rc);
 

@@ -81,7 +81,7 @@ __global__ void pack_kernel(const double* __restrict__ pos, const double* __rest
   out[i] = pack_body(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], c[0], c[1], c[2], w);
 }
 
-template <int T, int L, int BPT>
+template <int T, int L, int BPT, bool PACKED>
 __global__ void __launch_bounds__(T) rhs_mixed_kernel(const PackedBody* __restrict__ packed,
                                                       const double* __restrict__ vel,
                                                       double* __restrict__ out_vel,
@@ -89,16 +89,24 @@ __global__ void __launch_bounds__(T) rhs_mixed_kernel(const PackedBody* __restri
                                                       long long n, float eps2, double mass,
                                                       int uniform_mass) {
   constexpr int BI = (T / L) * BPT;
-  __shared__ PackedBody sh[T];
+  constexpr int SH = (PACKED ? (int)sizeof(PairRec) : (int)sizeof(PackedBody)) * T;
+  __shared__ __align__(16) unsigned char sh_raw[SH];
   __shared__ double part[BI][3];
   const ClusterInfo ci = cluster_info();
   const long long i0 = ci.itile * BI;
   long long jb, je;
   j_chunk(n, ci.rank, ci.size, T, jb, je);
-  if (uniform_mass)
-    force_mixed_cta<T, L, BPT, true>(packed, n, i0, jb, je, eps2, sh, part);
-  else
-    force_mixed_cta<T, L, BPT, false>(packed, n, i0, jb, je, eps2, sh, part);
+  if constexpr (PACKED) {
+    static_assert(BPT == 2, "packed path carries two bodies per thread");
+    force_mixed_cta_x2<T, L>(packed, n, i0, jb, je, eps2, reinterpret_cast<PairRec*>(sh_raw),
+                             part);
+  } else {
+    PackedBody* sh = reinterpret_cast<PackedBody*>(sh_raw);
+    if (uniform_mass)
+      force_mixed_cta<T, L, BPT, true>(packed, n, i0, jb, je, eps2, sh, part);
+    else
+      force_mixed_cta<T, L, BPT, false>(packed, n, i0, jb, je, eps2, sh, part);
+  }
   cluster_combine<BI>(part, ci.rank, ci.size);
   if (ci.rank != 0) return;
   const long long nb = min((long long)BI, n - i0);
@@ -122,25 +130,33 @@ const void* pick_f64(int L) {
   }
 }
 
-template <int T, int BPT>
+template <int T, int BPT, bool PACKED>
 const void* pick_mixed_L(int L) {
   switch (L) {
-    case 1: return (const void*)rhs_mixed_kernel<T, 1, BPT>;
-    case 2: return (const void*)rhs_mixed_kernel<T, 2, BPT>;
-    case 4: return (const void*)rhs_mixed_kernel<T, 4, BPT>;
-    case 8: return (const void*)rhs_mixed_kernel<T, 8, BPT>;
+    case 1: return (const void*)rhs_mixed_kernel<T, 1, BPT, PACKED>;
+    case 2: return (const void*)rhs_mixed_kernel<T, 2, BPT, PACKED>;
+    case 4: return (const void*)rhs_mixed_kernel<T, 4, BPT, PACKED>;
+    case 8: return (const void*)rhs_mixed_kernel<T, 8, BPT, PACKED>;
     default: return nullptr;
   }
 }
 
+// packed: the f32x2 path (two bodies per thread, uniform masses)
 template <int T>
-const void* pick_mixed(int L, int BPT) {
+const void* pick_mixed(int L, int BPT, bool packed = false) {
+  if (packed && BPT == 2) return pick_mixed_L<T, 2, true>(L);
   switch (BPT) {
-    case 1: return pick_mixed_L<T, 1>(L);
-    case 2: return pick_mixed_L<T, 2>(L);
-    case 4: return pick_mixed_L<T, 4>(L);
+    case 1: return pick_mixed_L<T, 1, false>(L);
+    case 2: return pick_mixed_L<T, 2, false>(L);
+    case 4: return pick_mixed_L<T, 4, false>(L);
     default: return nullptr;
   }
+}
+
+// The packed path is used for uniform masses with two bodies per thread
+// unless the tiling asks for the scalar path (reserved == 1).
+bool use_packed(const gb_force_tiling* tiling, int BPT, const double* masses) {
+  return BPT == 2 && !masses && !(tiling && tiling->reserved == 1);
 }
 
 int validate_nbody(const void* a, const void* b, long long n, double softening, double mass,
@@ -188,9 +204,9 @@ int rhs_for_start(int prec, const double* x, double* dxdt, long long n, double s
   ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
   const void* k = nullptr;
   switch (g.T) {
-    case 64: k = pick_mixed<64>(g.L, g.BPT); break;
-    case 128: k = pick_mixed<128>(g.L, g.BPT); break;
-    case 256: k = pick_mixed<256>(g.L, g.BPT); break;
+    case 64: k = pick_mixed<64>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
+    case 128: k = pick_mixed<128>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
+    case 256: k = pick_mixed<256>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
   }
   if (!k) return GB_ERR_UNSUPPORTED;
   const double* vel = x + 3 * n;
@@ -304,9 +320,9 @@ int mixed_rhs_into(const double* x, double* dxdt, long long n, double softening,
   ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
   const void* k = nullptr;
   switch (g.T) {
-    case 64: k = pick_mixed<64>(g.L, g.BPT); break;
-    case 128: k = pick_mixed<128>(g.L, g.BPT); break;
-    case 256: k = pick_mixed<256>(g.L, g.BPT); break;
+    case 64: k = pick_mixed<64>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
+    case 128: k = pick_mixed<128>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
+    case 256: k = pick_mixed<256>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
   }
   if (!k) return GB_ERR_UNSUPPORTED;
   const double* vel = x + 3 * n;
@@ -459,9 +475,9 @@ extern "C" int gb_nbody_rhs_mixed(const double* x, double* dxdt, int64_t n, doub
   ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
   const void* k = nullptr;
   switch (g.T) {
-    case 64: k = pick_mixed<64>(g.L, g.BPT); break;
-    case 128: k = pick_mixed<128>(g.L, g.BPT); break;
-    case 256: k = pick_mixed<256>(g.L, g.BPT); break;
+    case 64: k = pick_mixed<64>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
+    case 128: k = pick_mixed<128>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
+    case 256: k = pick_mixed<256>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
   }
   if (!k) return GB_ERR_UNSUPPORTED;
   const double* vel = x + 3 * n;
