@@ -385,13 +385,14 @@ typedef struct {
 
 typedef struct {
   int32_t precision;         /* GB_PREC_* */
-  int32_t controller;        /* GB_CTRL_REFERENCE or GB_CTRL_PI */
+  int32_t controller;        /* GB_CTRL_* */
   int32_t fsal;
   int32_t attempts_per_sync; /* attempts per graph replay (0 = 8) */
   int64_t max_attempts;      /* per system, 0 = unlimited */
   double host_wait_timeout_s;
   double pi_beta;
   gb_batch_tiling tiling;
+  const void* mlp;           /* gb_mlp* (host) for GB_CTRL_LEARNED */
 } gb_batch_opts;
 
 typedef struct gb_batch_s* gb_batch;

@@ -806,6 +806,8 @@ extern "C" int gb_batch_stats(gb_batch b, gb_integrate_stats* totals, gb_integra
     s.interactions = (double)c.n_rhs * (double)b->n[k] * (double)(b->n[k] - 1);
     s.status = c.status;
     s.done = c.done;
+    s.n_learned_proposals = c.n_learned;
+    s.n_learned_rejected = c.n_learned_rejected;
     if (per_sys) per_sys[k] = s;
     tot.n_accepted += s.n_accepted;
     tot.n_rejected += s.n_rejected;
@@ -813,6 +815,8 @@ extern "C" int gb_batch_stats(gb_batch b, gb_integrate_stats* totals, gb_integra
     tot.n_rhs += s.n_rhs;
     tot.n_rhs_saved += s.n_rhs_saved;
     tot.interactions += s.interactions;
+    tot.n_learned_proposals += s.n_learned_proposals;
+    tot.n_learned_rejected += s.n_learned_rejected;
     tot.t = std::min(tot.t, s.t);
     if (s.status != GB_OK) tot.status = s.status;
   }

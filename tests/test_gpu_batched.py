@@ -63,3 +63,53 @@ def test_batch_budget_status(gb, torch_cuda):
     st = b.stats(per_system=True)
     assert all(s["n_attempts"] == 3 for s in st["systems"])
     b.close()
+
+
+def _zero_mlp(gb):
+    """A network whose output is exactly zero: the learned proposal is then
+    the elementary controller's formula in log form."""
+    import ctypes as C
+    m = gb.GbMlp()
+    assert gb.lib().gb_mlp_init(C.byref(m), 9) == 0
+    for k in range(64):
+        m.w3[k] = 0.0
+    m.b3 = 0.0
+    m.out_bias = 0.0
+    m.out_scale = 1.0
+    for k in range(16):
+        m.in_scale[k] = 1.0
+    return m
+
+
+def test_batch_learned_controller(gb, torch_cuda):
+    """The batched control warp evaluates the proposer per system; with a
+    zero-output network every system takes the same accepted steps as the
+    single-system integrator under the same network."""
+    sizes = [48, 96, 160]
+    soft, tol, tf = 0.05, 1e-9, 0.1
+    xs, x0 = _systems(gb, sizes, 70)
+    m = _zero_mlp(gb)
+    b = gb.Batch("DOPRI5", sizes, soft, precision="f64", controller="learned", mlp=m)
+    b.start(x0, 0.0, tf, tol, tol)
+    assert b.advance() == 0
+    st = b.stats(per_system=True)
+    assert st["n_learned_proposals"] > 0
+    x, t = b.state()
+    x = x.cpu().numpy()
+    np.testing.assert_allclose(t, tf)
+    for k, n in enumerate(sizes):
+        exe = gb.Gb300Executor(precision="f64", controller="learned", mlp=m)
+        it = gb.Integrator("DOPRI5", gb.NBodyODE(n, soft, 1.0 / n), exe)
+        it.start(xs[k], 0.0, tf, tol, tol)
+        assert it.advance(0) == 0
+        s1 = it.stats()
+        assert abs(st["systems"][k]["n_accepted"] - s1["n_accepted"]) <= 1, k
+        xk, _ = it.state()
+        assert np.max(np.abs(b.system_state(x, k) - xk.cpu().numpy())) <= 10 * tol
+        it.close()
+    b.close()
+
+
+def test_batch_learned_requires_network(gb, torch_cuda):
+    with pytest.raises(gb.GbError):
+        gb.Batch("DOPRI5", [32], 0.05, precision="f64", controller="learned")
