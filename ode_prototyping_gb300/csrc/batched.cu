@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(T)
     const long long nb = min((long long)BI, n - i0);
     double sq_acc = 0.0, amax = 0.0;
     for (int b = threadIdx.x; b < nb; b += T) body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
-    if (s == 0 && !skip_force) {
+    if (last) {
       const double m = block_max(amax, red);
       if (threadIdx.x == 0) P.aux[u] = m;
     }
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(128)
   int want = 0;
   if (lane == 0) {
     Ctrl pre = *C;
-    if (!pre.k0_valid) pre.max_abs_acc = m;
+    pre.max_abs_acc = m;
     want = P.mlp && pre.controller == GB_CTRL_LEARNED && isfinite(err) && err <= 1.0;
     if (want) {
       preview_history(pre, err, true);
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(128)
   if (lane == 0) {
     Ctrl c = *C;
     const int k0_valid = c.k0_valid;
-    if (!k0_valid) c.max_abs_acc = m;
+    c.max_abs_acc = m;
     c.n_rhs += k0_valid ? S - 1 : S;
     if (k0_valid) c.n_rhs_saved += 1;
     const CtrlEnv env{nullptr, 0, nullptr, 2, sy.n};

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(T)
   double sq_acc = 0.0;
   double amax = 0.0;
   for (int b = threadIdx.x; b < nb; b += T) body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
-  if (s == 0 && !skip_force) {
+  if (last) {
     const double m = block_max(amax, red);
     if (threadIdx.x == 0) P.aux[ci.itile] = m;
   }
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(T, 1024 / T)
   TileMeta* meta_out = (last ? P.MX : P.MY) + po * nt + ci.itile;
   const float w = valid ? (P.masses ? (float)P.masses[id] : 1.0f) : 0.f;
   pack_sorted_tile(np, valid, (int)nb, w, P.cref, near_out, far_out, meta_out, red);
-  if (s == 0 && !skip_force) {
+  if (last) {
     const double m = block_max(amax, red);
     if (threadIdx.x == 0) P.aux[ci.itile] = m;
   }
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(256)
   }
   const int k0_valid = C->k0_valid;
   double amax_all = 0.0;
-  if (!k0_valid) {
+  {
     double v = 0.0;
     for (long long k = threadIdx.x; k < P.n_itiles; k += T) v = fmax(v, P.aux[k]);
     amax_all = block_max(v, red);
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(256)
   // the 16 -> 64 -> 64 -> 1 network across the CTA.
   if (threadIdx.x == 0) {
     Ctrl c = *C;
-    if (!k0_valid) c.max_abs_acc = amax_all;
+    c.max_abs_acc = amax_all;
     const bool want = P.mlp && c.controller == GB_CTRL_LEARNED && isfinite(err) && err <= 1.0;
     sh_flag = want ? 1 : 0;
     if (want) {
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256)
   }
   if (threadIdx.x == 0) {
     Ctrl c = *C;
-    if (!k0_valid) c.max_abs_acc = amax_all;
+    c.max_abs_acc = amax_all;
     c.n_rhs += k0_valid ? S - 1 : S;
     if (k0_valid) c.n_rhs_saved += 1;
     const CtrlEnv env{P.log, P.log_capacity, P.times_ring, P.R, P.n};

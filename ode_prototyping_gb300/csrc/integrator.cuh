@@ -15,7 +15,7 @@ struct Ctrl {
   double safety;      // 0.38^(1/(1+q)) (RKEmbeddedParallel.hpp:24)
   double dt_initial;
   double pi_alpha, pi_beta;
-  double max_abs_acc; // max |a| over bodies in the last attempt's first stage
+  double max_abs_acc; // max |a| over bodies at the last attempt's final stage
   double min_r2;      // min pair separation^2 seen in the last first stage (learned features)
   double dt_hist[3];  // last three attempted step sizes
   double err_hist[3]; // last three error norms

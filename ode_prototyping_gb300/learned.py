@@ -28,17 +28,27 @@ import time
 import numpy as np
 
 from . import (GbMlp, GbIntegrateStats, Gb300Executor, Integrator, NBodyODE, check, energy,
-               ic_plummer, lib, tableau)
+               ic_binary_plummer, ic_plummer, lib, tableau)
 
 FEAT, LOG_DT, LOG_ERR, ACCEPTED = slice(0, 16), 16, 17, 18
 
 
+def initial_state(kind: str, n: int, seed: int) -> np.ndarray:
+    """'plummer': Plummer sphere; 'binary': Plummer sphere with 10% of the
+    bodies in bound pairs, semimajor axes log-uniform in [1e-3, 1e-2]."""
+    if kind == "plummer":
+        return ic_plummer(n, seed)
+    if kind == "binary":
+        return ic_binary_plummer(n, seed, 0.1, 1e-3, 1e-2)
+    raise ValueError(f"unknown initial state {kind!r}")
+
+
 def collect_logs(seeds, n: int, softening: float, tab: str, tol: float, tf: float,
                  attempts: int, precision: str = "mixed", controller: str = "reference",
-                 mlp: GbMlp | None = None):
+                 mlp: GbMlp | None = None, ic: str = "plummer"):
     logs = []
     for seed in seeds:
-        x0 = ic_plummer(n, seed)
+        x0 = initial_state(ic, n, seed)
         exe = Gb300Executor(precision=precision, controller=controller, attempts_per_sync=16,
                             log_steps=attempts, mlp=mlp)
         it = Integrator(tab, NBodyODE(n, softening, 1.0 / n), exe)
@@ -104,19 +114,21 @@ def train(x: np.ndarray, y: np.ndarray, epochs: int = 3000, lr: float = 3e-3,
 
 
 def fit(seeds, n: int, softening: float, tab: str, tol: float, tf: float, attempts: int,
-        rounds: int = 2, rho: float = 0.6, epochs: int = 3000, over_weight: float = 2.0):
+        rounds: int = 2, rho: float = 0.6, epochs: int = 3000, over_weight: float = 2.0,
+        ic: str = "plummer"):
     """Logs of the reference and PI controllers, a first fit, then rounds of
     logs collected under the learned controller itself (so the data cover the
     states it visits) and refits.  Returns (network, info)."""
     q = min(tableau(tab).p, tableau(tab).pt)
-    logs = collect_logs(seeds, n, softening, tab, tol, tf, attempts, controller="reference")
-    logs += collect_logs(seeds, n, softening, tab, tol, tf, attempts, controller="pi")
+    logs = collect_logs(seeds, n, softening, tab, tol, tf, attempts, controller="reference",
+                        ic=ic)
+    logs += collect_logs(seeds, n, softening, tab, tol, tf, attempts, controller="pi", ic=ic)
     info = []
     m = None
     for r in range(max(rounds, 1)):
         if m is not None:
             logs += collect_logs(seeds, n, softening, tab, tol, tf, attempts,
-                                 controller="learned", mlp=m)
+                                 controller="learned", mlp=m, ic=ic)
         x, y = build_dataset(logs, q, rho)
         m, loss = train(x, y, epochs=epochs, over_weight=over_weight)
         info.append({"round": r, "samples": int(len(y)), "loss": loss})
@@ -124,9 +136,10 @@ def fit(seeds, n: int, softening: float, tab: str, tol: float, tf: float, attemp
 
 
 def run_window(n: int, softening: float, tab: str, tol: float, t_end: float, seed: int,
-               controller: str, mlp: GbMlp | None = None, precision: str = "mixed") -> dict:
+               controller: str, mlp: GbMlp | None = None, precision: str = "mixed",
+               ic: str = "plummer") -> dict:
     import torch
-    x0 = ic_plummer(n, seed)
+    x0 = initial_state(ic, n, seed)
     stream = torch.cuda.Stream()
     exe = Gb300Executor(precision=precision, controller=controller, attempts_per_sync=16,
                         mlp=mlp)
@@ -152,11 +165,11 @@ def run_window(n: int, softening: float, tab: str, tol: float, t_end: float, see
             "energy_rel_err": abs(e1["e"] - e0["e"]) / abs(e0["e"]), "state": xs}
 
 
-def evaluate(n, softening, tab, tol, t_end, seeds, mlp, precision="mixed"):
+def evaluate(n, softening, tab, tol, t_end, seeds, mlp, precision="mixed", ic="plummer"):
     out = {}
     for ctl in ("reference", "pi", "learned"):
         rows = [run_window(n, softening, tab, tol, t_end, s, ctl,
-                           mlp if ctl == "learned" else None, precision) for s in seeds]
+                           mlp if ctl == "learned" else None, precision, ic) for s in seeds]
         agg = {k: float(np.sum([r[k] for r in rows])) for k in
                ("wall_s", "accepted", "rejected", "attempts", "rhs", "learned_proposals",
                 "learned_rejected")}
