@@ -48,6 +48,11 @@ WORKLOAD = {
 METRIC = "accepted steps/s and pair-interactions/s at equal energy error: learned+mixed vs FP64"
 FP32_LANES_PER_SM = 128
 FLOPS_PER_INTERACTION = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) convention
+# FP32-pipe operations per interaction of the hi/lo pair term: 9 for the three
+# (hj - hi) + (lj - li) differences, 3 FMA for r^2 + eps^2, 2 multiplies for
+# r^-3, 3 FMA accumulations (rsqrt runs on the SFU).  The 20-FLOP convention
+# counts 10 FMA-equivalents, so the FP32 pipe caps the fraction at 10/17.
+HILO_FP32_OPS = 17
 
 
 def peaks():
@@ -351,7 +356,9 @@ def main():
                      "kernel_ms": k_ms, "geometry": geo,
                      "peak_note": f"nominal FP32 pipe: {n_sm} SMs x {FP32_LANES_PER_SM} lanes x 2"
                                   f" x {sm_mhz_max:.0f} MHz ({pk_kind} peaks file has no FP32)",
-                     "flops_per_interaction": FLOPS_PER_INTERACTION},
+                     "flops_per_interaction": FLOPS_PER_INTERACTION,
+                     "fp32_ops_per_interaction": HILO_FP32_OPS,
+                     "fp32_pipe_cap_frac": FLOPS_PER_INTERACTION / 2 / HILO_FP32_OPS},
     }
     if rank == 0:
         line["e2e"] = e2e(gb, torch, x0)

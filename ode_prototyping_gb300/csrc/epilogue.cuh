@@ -67,7 +67,7 @@ struct EpiCtx {
 
 // One body's six state elements.  `acc` is the unscaled pair sum (ignored
 // when the stage derivative is reused).  Adds the body's scaled squares to
-// sq_acc (last stage) and its |a| to amax (stage 0).
+// sq_acc and its |a| to amax (both at the last stage).
 template <int PREC>
 __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, const double* acc,
                                               double& sq_acc, double& amax,
@@ -94,7 +94,7 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
     }
 #pragma unroll
     for (int e = 0; e < 6; ++e) ks_s[idx[e]] = k[e];
-    if (s == 0) amax = fmax(amax, sqrt(k[3] * k[3] + k[4] * k[4] + k[5] * k[5]));
+    if (E.last) amax = fmax(amax, sqrt(k[3] * k[3] + k[4] * k[4] + k[5] * k[5]));
   }
   if (!E.last) {
     double yn[6];

@@ -9,6 +9,7 @@
 // ascending, then x0 + sum * dt) with IEEE-rounded operations, so the results
 // equal the reference's element for element; coefficients that are exactly
 // zero are skipped, which can only change the sign of a zero result.
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 
@@ -68,43 +69,119 @@ unsigned blocks_for(long long n) {
   return (unsigned)b;
 }
 
-__global__ void stage_kernel(const __grid_constant__ DevTableau tab, int stage, double dt,
-                             const double* __restrict__ x0, const double* __restrict__ ks,
-                             double* __restrict__ temp, long long n) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double v = 0.0;
-  for (int j = 0; j < stage; ++j) {
-    const double a = tab.a[stage - 1][j];
-    if (a != 0.0) v = dadd(v, dmul(a, ks[j * n + i]));
+// One linear combination's coefficients, uniform across the grid: c[j] for
+// the sum written to the first output, d[j] for an optional second one.
+struct Coef {
+  double c[GB_MAX_STAGES];
+  double d[GB_MAX_STAGES];
+};
+
+// V consecutive doubles per thread and iteration (V = 2: 16-byte loads).
+template <int V>
+struct Vec;
+template <>
+struct Vec<1> {
+  double v[1];
+  __device__ __forceinline__ void load(const double* __restrict__ p, long long e) { v[0] = p[e]; }
+  __device__ __forceinline__ void store(double* __restrict__ p, long long e) const { p[e] = v[0]; }
+};
+template <>
+struct Vec<2> {
+  double v[2];
+  __device__ __forceinline__ void load(const double* __restrict__ p, long long e) {
+    const double2 t = reinterpret_cast<const double2*>(p)[e];
+    v[0] = t.x;
+    v[1] = t.y;
   }
-  temp[i] = dadd(x0[i], dmul(v, dt));
+  __device__ __forceinline__ void store(double* __restrict__ p, long long e) const {
+    reinterpret_cast<double2*>(p)[e] = make_double2(v[0], v[1]);
+  }
+};
+
+// temp = x0 + dt * sum_{j<S} c[j] k_j (rk_stage_kernel, RKEmbeddedParallel.hpp:91-101).
+// Every k_j with a non-zero coefficient is loaded before the ordered sum, so
+// S loads per element are in flight at once; the sum itself keeps the
+// reference's order (from 0.0, j ascending, then * dt, then + x0).
+template <int S, int V>
+__global__ void __launch_bounds__(kBlock) stage_kernel(const __grid_constant__ Coef cf, double dt,
+                                                       const double* __restrict__ x0,
+                                                       const double* __restrict__ ks,
+                                                       double* __restrict__ temp, long long n) {
+  const long long m = n / V;
+  for (long long e = blockIdx.x * (long long)kBlock + threadIdx.x; e < m;
+       e += (long long)gridDim.x * kBlock) {
+    Vec<V> k[S], x;
+#pragma unroll
+    for (int j = 0; j < S; ++j)
+      if (cf.c[j] != 0.0) k[j].load(ks + (long long)j * n, e);
+    x.load(x0, e);
+    Vec<V> out;
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      double v = 0.0;
+#pragma unroll
+      for (int j = 0; j < S; ++j)
+        if (cf.c[j] != 0.0) v = dadd(v, dmul(cf.c[j], k[j].v[u]));
+      out.v[u] = dadd(x.v[u], dmul(v, dt));
+    }
+    out.store(temp, e);
+  }
 }
 
-__global__ void update_kernel(const __grid_constant__ DevTableau tab, double dt,
-                              const double* __restrict__ x0, const double* __restrict__ ks,
-                              double* __restrict__ x, double* __restrict__ err, long long n) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double xv = 0.0, ev = 0.0;
-  for (int j = 0; j < tab.n_stages; ++j) {
-    const double b = tab.b[j], db = tab.db[j];
-    if (b == 0.0 && db == 0.0) continue;
-    const double k = ks[j * n + i];
-    if (b != 0.0) xv = dadd(xv, dmul(b, k));
-    if (db != 0.0) ev = dadd(ev, dmul(db, k));
+// x = x0 + dt * sum b_j k_j, err = dt * sum (b_j - bt_j) k_j
+// (update_state_and_error_kernel, RKEmbeddedParallel.hpp:103-123).
+template <int S, int V>
+__global__ void __launch_bounds__(kBlock) update_kernel(const __grid_constant__ Coef cf, double dt,
+                                                        const double* __restrict__ x0,
+                                                        const double* __restrict__ ks,
+                                                        double* __restrict__ x,
+                                                        double* __restrict__ err, long long n) {
+  const long long m = n / V;
+  for (long long e = blockIdx.x * (long long)kBlock + threadIdx.x; e < m;
+       e += (long long)gridDim.x * kBlock) {
+    Vec<V> k[S], x0v;
+#pragma unroll
+    for (int j = 0; j < S; ++j)
+      if (cf.c[j] != 0.0 || cf.d[j] != 0.0) k[j].load(ks + (long long)j * n, e);
+    x0v.load(x0, e);
+    Vec<V> xo, eo;
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      double xv = 0.0, ev = 0.0;
+#pragma unroll
+      for (int j = 0; j < S; ++j) {
+        if (cf.c[j] != 0.0) xv = dadd(xv, dmul(cf.c[j], k[j].v[u]));
+        if (cf.d[j] != 0.0) ev = dadd(ev, dmul(cf.d[j], k[j].v[u]));
+      }
+      xo.v[u] = dadd(x0v.v[u], dmul(xv, dt));
+      eo.v[u] = dmul(ev, dt);
+    }
+    xo.store(x, e);
+    eo.store(err, e);
   }
-  x[i] = dadd(x0[i], dmul(xv, dt));
-  err[i] = dmul(ev, dt);
 }
 
-__global__ void target_kernel(const double* __restrict__ atol, const double* __restrict__ rtol,
-                              const double* __restrict__ x, const double* __restrict__ x0,
-                              double* __restrict__ target, long long n) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double a = fabs(x[i]), b = fabs(x0[i]);
-  target[i] = dadd(atol[i], dmul(rtol[i], a < b ? b : a));
+template <int V>
+__global__ void __launch_bounds__(kBlock) target_kernel(const double* __restrict__ atol,
+                                                        const double* __restrict__ rtol,
+                                                        const double* __restrict__ x,
+                                                        const double* __restrict__ x0,
+                                                        double* __restrict__ target, long long n) {
+  const long long m = n / V;
+  for (long long e = blockIdx.x * (long long)kBlock + threadIdx.x; e < m;
+       e += (long long)gridDim.x * kBlock) {
+    Vec<V> at, rt, xv, x0v, out;
+    at.load(atol, e);
+    rt.load(rtol, e);
+    xv.load(x, e);
+    x0v.load(x0, e);
+#pragma unroll
+    for (int u = 0; u < V; ++u) {
+      const double a = fabs(xv.v[u]), b = fabs(x0v.v[u]);
+      out.v[u] = dadd(at.v[u], dmul(rt.v[u], a < b ? b : a));
+    }
+    out.store(target, e);
+  }
 }
 
 __global__ void fill_kernel(double* p, long long n, double v) {
@@ -121,18 +198,33 @@ int norm_blocks(long long n) {
   return (int)b;
 }
 
-// Per-block partial sums of (v/s)^2: grid-stride per thread, then a fixed
-// shared-memory tree.  Deterministic for a given n.
-__global__ void sq_partial_kernel(const double* __restrict__ v, const double* __restrict__ s,
-                                  long long n, double* __restrict__ partial) {
+// Per-block partial sums of (v/s)^2: each thread keeps four independent
+// running sums over a grid-stride walk (four IEEE divisions in flight), adds
+// them in a fixed order, then a fixed shared-memory tree.  Deterministic for
+// a given n.
+__global__ void __launch_bounds__(kBlock) sq_partial_kernel(const double* __restrict__ v,
+                                                            const double* __restrict__ s,
+                                                            long long n,
+                                                            double* __restrict__ partial) {
   __shared__ double sh[kBlock];
-  double acc = 0.0;
-  for (long long i = blockIdx.x * (long long)kBlock + threadIdx.x; i < n;
-       i += (long long)gridDim.x * kBlock) {
-    const double q = __ddiv_rn(v[i], s[i]);
-    acc = dadd(acc, dmul(q, q));
+  constexpr int U = 4;
+  double acc[U] = {0.0, 0.0, 0.0, 0.0};
+  const long long stride = (long long)gridDim.x * kBlock;
+  for (long long i0 = blockIdx.x * (long long)kBlock + threadIdx.x; i0 < n; i0 += U * stride) {
+    double vv[U], ss[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long i = i0 + u * stride;
+      vv[u] = i < n ? v[i] : 0.0;
+      ss[u] = i < n ? s[i] : 1.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const double q = __ddiv_rn(vv[u], ss[u]);
+      acc[u] = dadd(acc[u], dmul(q, q));
+    }
   }
-  sh[threadIdx.x] = acc;
+  sh[threadIdx.x] = dadd(dadd(acc[0], acc[1]), dadd(acc[2], acc[3]));
   __syncthreads();
   for (int st = kBlock / 2; st > 0; st /= 2) {
     if ((int)threadIdx.x < st) sh[threadIdx.x] = dadd(sh[threadIdx.x], sh[threadIdx.x + st]);
@@ -154,6 +246,50 @@ __global__ void sq_final_kernel(const double* __restrict__ partial, int nb, long
     __syncthreads();
   }
   if (threadIdx.x == 0) *out = take_sqrt ? sqrt(sh[0] / (double)n) : sh[0];
+}
+
+}  // namespace
+
+namespace {
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// Persistent-style grid for the streaming kernels: at most 8 blocks of 256
+// threads per SM (all resident), grid-stride beyond that.
+unsigned stream_blocks(long long m) {
+  long long b = (m + kBlock - 1) / kBlock;
+  const long long cap = (long long)num_sms() * 8;
+  if (b > cap) b = cap;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+#define GB_STAGE_CASES(X) \
+  X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16)
+
+template <int V>
+void launch_stage_v(int S, const Coef& cf, double dt, const double* x0, const double* ks,
+                    double* temp, long long n, cudaStream_t st) {
+  const unsigned g = stream_blocks(n / V);
+  switch (S) {
+#define GB_CASE(k) \
+  case k: stage_kernel<k, V><<<g, kBlock, 0, st>>>(cf, dt, x0, ks, temp, n); break;
+    GB_STAGE_CASES(GB_CASE)
+#undef GB_CASE
+    default: break;
+  }
+}
+
+template <int V>
+void launch_update_v(int S, const Coef& cf, double dt, const double* x0, const double* ks,
+                     double* x, double* err, long long n, cudaStream_t st) {
+  const unsigned g = stream_blocks(n / V);
+  switch (S) {
+#define GB_CASE(k) \
+  case k: update_kernel<k, V><<<g, kBlock, 0, st>>>(cf, dt, x0, ks, x, err, n); break;
+    GB_STAGE_CASES(GB_CASE)
+#undef GB_CASE
+    default: break;
+  }
 }
 
 }  // namespace
@@ -355,8 +491,14 @@ extern "C" int gb_rk_stage_f64(const gb_tableau* tab, int32_t stage, double dt, 
   GB_TRY(check_tableau(tab));
   if (!x0 || !ks || !temp || n < 1 || stage < 1 || stage >= tab->n_stages)
     return GB_ERR_INVALID_ARGUMENT;
-  stage_kernel<<<blocks_for(n), kBlock, 0, as_cuda(stream)>>>(make_dev_tableau(*tab), stage, dt,
-                                                              x0, ks, temp, n);
+  Coef cf;
+  std::memset(&cf, 0, sizeof cf);
+  for (int j = 0; j < stage; ++j) cf.c[j] = tab->a[stage - 1][j];
+  cudaStream_t st = as_cuda(stream);
+  if (n % 2 == 0 && aligned16(x0) && aligned16(ks) && aligned16(temp))
+    launch_stage_v<2>(stage, cf, dt, x0, ks, temp, n, st);
+  else
+    launch_stage_v<1>(stage, cf, dt, x0, ks, temp, n, st);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -366,8 +508,17 @@ extern "C" int gb_rk_update_state_and_error_f64(const gb_tableau* tab, double dt
                                                 double* err, int64_t n, gb_stream_t stream) {
   GB_TRY(check_tableau(tab));
   if (!x0 || !ks || !x || !err || n < 1) return GB_ERR_INVALID_ARGUMENT;
-  update_kernel<<<blocks_for(n), kBlock, 0, as_cuda(stream)>>>(make_dev_tableau(*tab), dt, x0,
-                                                               ks, x, err, n);
+  Coef cf;
+  std::memset(&cf, 0, sizeof cf);
+  for (int j = 0; j < tab->n_stages; ++j) {
+    cf.c[j] = tab->b[j];
+    cf.d[j] = tab->b[j] - tab->bt[j];
+  }
+  cudaStream_t st = as_cuda(stream);
+  if (n % 2 == 0 && aligned16(x0) && aligned16(ks) && aligned16(x) && aligned16(err))
+    launch_update_v<2>(tab->n_stages, cf, dt, x0, ks, x, err, n, st);
+  else
+    launch_update_v<1>(tab->n_stages, cf, dt, x0, ks, x, err, n, st);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -376,7 +527,12 @@ extern "C" int gb_rk_error_target_f64(const double* atol, const double* rtol, co
                                       const double* x0, double* target, int64_t n,
                                       gb_stream_t stream) {
   if (!atol || !rtol || !x || !x0 || !target || n < 1) return GB_ERR_INVALID_ARGUMENT;
-  target_kernel<<<blocks_for(n), kBlock, 0, as_cuda(stream)>>>(atol, rtol, x, x0, target, n);
+  cudaStream_t st = as_cuda(stream);
+  if (n % 2 == 0 && aligned16(atol) && aligned16(rtol) && aligned16(x) && aligned16(x0) &&
+      aligned16(target))
+    target_kernel<2><<<stream_blocks(n / 2), kBlock, 0, st>>>(atol, rtol, x, x0, target, n);
+  else
+    target_kernel<1><<<stream_blocks(n), kBlock, 0, st>>>(atol, rtol, x, x0, target, n);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
