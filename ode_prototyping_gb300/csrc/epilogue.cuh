@@ -96,18 +96,34 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
     for (int e = 0; e < 6; ++e) ks_s[idx[e]] = k[e];
     if (E.last) amax = fmax(amax, sqrt(k[3] * k[3] + k[4] * k[4] + k[5] * k[5]));
   }
+  // Stage sums: the stage index runs outermost so that a stage's six loads
+  // are in flight together; every element still sums its terms from 0.0 in
+  // ascending stage order.
+  double x0v[6];
+#pragma unroll
+  for (int e = 0; e < 6; ++e) x0v[e] = E.x0[idx[e]];
   if (!E.last) {
-    double yn[6];
+    double yn[6], v[6];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) v[e] = 0.0;
+    for (int l = 0; l <= s; ++l) {
+      const double a = tab.a[s][l];
+      if (a == 0.0) continue;
+      double kl[6];
+      if (l == s) {
+#pragma unroll
+        for (int e = 0; e < 6; ++e) kl[e] = k[e];
+      } else {
+        const double* kp = E.ks + (long long)kslot(l, S, E.k0slot) * E.kstride;
+#pragma unroll
+        for (int e = 0; e < 6; ++e) kl[e] = kp[idx[e]];
+      }
+#pragma unroll
+      for (int e = 0; e < 6; ++e) v[e] = dadd(v[e], dmul(a, kl[e]));
+    }
 #pragma unroll
     for (int e = 0; e < 6; ++e) {
-      double v = 0.0;
-      for (int l = 0; l <= s; ++l) {
-        const double a = tab.a[s][l];
-        if (a == 0.0) continue;
-        const double kl = (l == s) ? k[e] : E.ks[(long long)kslot(l, S, E.k0slot) * E.kstride + idx[e]];
-        v = dadd(v, dmul(a, kl));
-      }
-      yn[e] = dadd(E.x0[idx[e]], dmul(v, E.dt));
+      yn[e] = dadd(x0v[e], dmul(v[e], E.dt));
       E.ynext[idx[e]] = yn[e];
     }
     if (newpos) {
@@ -119,20 +135,32 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
       E.pnext[i] = pack_body(yn[0], yn[1], yn[2], E.cref[0], E.cref[1], E.cref[2], w);
     }
   } else {
-    double xn[6];
+    double xn[6], xv[6], ev[6];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) xv[e] = ev[e] = 0.0;
+    for (int l = 0; l < S; ++l) {
+      const double bb = tab.b[l], db = tab.db[l];
+      if (bb == 0.0 && db == 0.0) continue;
+      double kl[6];
+      if (l == s) {
+#pragma unroll
+        for (int e = 0; e < 6; ++e) kl[e] = k[e];
+      } else {
+        const double* kp = E.ks + (long long)kslot(l, S, E.k0slot) * E.kstride;
+#pragma unroll
+        for (int e = 0; e < 6; ++e) kl[e] = kp[idx[e]];
+      }
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        if (bb != 0.0) xv[e] = dadd(xv[e], dmul(bb, kl[e]));
+        if (db != 0.0) ev[e] = dadd(ev[e], dmul(db, kl[e]));
+      }
+    }
 #pragma unroll
     for (int e = 0; e < 6; ++e) {
-      double xv = 0.0, ev = 0.0;
-      for (int l = 0; l < S; ++l) {
-        const double bb = tab.b[l], db = tab.db[l];
-        if (bb == 0.0 && db == 0.0) continue;
-        const double kl = (l == s) ? k[e] : E.ks[(long long)kslot(l, S, E.k0slot) * E.kstride + idx[e]];
-        if (bb != 0.0) xv = dadd(xv, dmul(bb, kl));
-        if (db != 0.0) ev = dadd(ev, dmul(db, kl));
-      }
-      const double x0e = E.x0[idx[e]];
-      xn[e] = dadd(x0e, dmul(xv, E.dt));
-      const double er = dmul(ev, E.dt);
+      const double x0e = x0v[e];
+      xn[e] = dadd(x0e, dmul(xv[e], E.dt));
+      const double er = dmul(ev[e], E.dt);
       E.xnew[idx[e]] = xn[e];
       const double at = E.atol ? E.atol[idx[e]] : E.atol_s;
       const double rt = E.rtol ? E.rtol[idx[e]] : E.rtol_s;

@@ -223,27 +223,59 @@ __device__ __forceinline__ void force_mixed_cta(const PackedBody* __restrict__ p
     float tx[BPT], ty[BPT], tz[BPT];
 #pragma unroll
     for (int q = 0; q < BPT; ++q) tx[q] = ty[q] = tz[q] = 0.f;
+    // Same scheme as the packed path: hi-only terms without branching, close
+    // pairs marked per chunk of 32 partners and replaced afterwards.
+    const int kn = (cnt - l + L - 1) / L;
+    for (int k0 = 0; k0 < kn; k0 += 32) {
+      const int kc = min(32, kn - k0);
+      unsigned mask = 0;
 #pragma unroll 4
-    for (int jj = l; jj < cnt; jj += L) {
-      const float4 hw = sh[jj].hw;
-      const float4 lo = sh[jj].lo;
+      for (int u = 0; u < kc; ++u) {
+        const int jj = l + (k0 + u) * L;
+        const float4 hw = sh[jj].hw;
+        bool close = false;
 #pragma unroll
-      for (int q = 0; q < BPT; ++q) {
-        float dx = hw.x - hx[q];
-        float dy = hw.y - hy[q];
-        float dz = hw.z - hz[q];
-        float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
-        if (__float_as_int(r2) < near2[q]) {  // close pair: add the lo parts
+        for (int q = 0; q < BPT; ++q) {
+          const float dx = hw.x - hx[q];
+          const float dy = hw.y - hy[q];
+          const float dz = hw.z - hz[q];
+          const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+          close |= __float_as_int(r2) < near2[q];
+          const float rinv = rsqrt_sfu(r2);
+          const float sc = UNIFORM ? rinv * (rinv * rinv) : (hw.w * rinv) * (rinv * rinv);
+          tx[q] = fmaf(sc, dx, tx[q]);
+          ty[q] = fmaf(sc, dy, ty[q]);
+          tz[q] = fmaf(sc, dz, tz[q]);
+        }
+        mask |= (unsigned)close << u;
+      }
+      while (mask) {
+        const int u = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int jj = l + (k0 + u) * L;
+        const float4 hw = sh[jj].hw;
+        const float4 lo = sh[jj].lo;
+#pragma unroll
+        for (int q = 0; q < BPT; ++q) {
+          float dx = hw.x - hx[q];
+          float dy = hw.y - hy[q];
+          float dz = hw.z - hz[q];
+          float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+          float rinv = rsqrt_sfu(r2);
+          float sc = UNIFORM ? rinv * (rinv * rinv) : (hw.w * rinv) * (rinv * rinv);
+          tx[q] = fmaf(-sc, dx, tx[q]);  // take the hi-only term out again
+          ty[q] = fmaf(-sc, dy, ty[q]);
+          tz[q] = fmaf(-sc, dz, tz[q]);
           dx = dx + (lo.x - lx[q]);
           dy = dy + (lo.y - ly[q]);
           dz = dz + (lo.z - lz[q]);
           r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
+          rinv = rsqrt_sfu(r2);
+          sc = UNIFORM ? rinv * (rinv * rinv) : (hw.w * rinv) * (rinv * rinv);
+          tx[q] = fmaf(sc, dx, tx[q]);
+          ty[q] = fmaf(sc, dy, ty[q]);
+          tz[q] = fmaf(sc, dz, tz[q]);
         }
-        const float rinv = rsqrt_sfu(r2);
-        const float s = UNIFORM ? rinv * (rinv * rinv) : (hw.w * rinv) * (rinv * rinv);
-        tx[q] = fmaf(s, dx, tx[q]);
-        ty[q] = fmaf(s, dy, ty[q]);
-        tz[q] = fmaf(s, dz, tz[q]);
       }
     }
 #pragma unroll
@@ -361,30 +393,62 @@ __device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict_
     __syncthreads();
     if (j0 + JT + threadIdx.x < je) nxt = packed[j0 + JT + threadIdx.x];
     f2_t TX = 0ULL, TY = 0ULL, TZ = 0ULL;  // bit pattern of (+0.f, +0.f)
+    // This lane's partners are jj = l + L k, k < kn.  The loop adds every
+    // pair's hi-only term without branching and marks close pairs in a
+    // 32-bit mask per chunk of 32 k; the marked pairs are then revisited:
+    // the hi-only term is taken out again and the hi/lo term added.
+    const int kn = (cnt - l + L - 1) / L;
+    for (int k0 = 0; k0 < kn; k0 += 32) {
+      const int kc = min(32, kn - k0);
+      unsigned mask = 0;
 #pragma unroll 4
-    for (int jj = l; jj < cnt; jj += L) {
-      const ulonglong2 xy = sh[jj].xy;
-      const ulonglong2 zl = sh[jj].zl;
-      f2_t dx = f2_sub(xy.x, HX);
-      f2_t dy = f2_sub(xy.y, HY);
-      f2_t dz = f2_sub(zl.x, HZ);
-      f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-      float ra, rb;
-      f2_unpack(r2, ra, rb);
-      if (__float_as_int(ra) < near_a || __float_as_int(rb) < near_b) {
-        // a close pair in either body: both take (hj - hi) + (lj - li)
+      for (int u = 0; u < kc; ++u) {
+        const int jj = l + (k0 + u) * L;
+        const ulonglong2 xy = sh[jj].xy;
+        const f2_t hz = sh[jj].zl.x;
+        const f2_t dx = f2_sub(xy.x, HX);
+        const f2_t dy = f2_sub(xy.y, HY);
+        const f2_t dz = f2_sub(hz, HZ);
+        const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+        float ra, rb;
+        f2_unpack(r2, ra, rb);
+        const bool close = (__float_as_int(ra) < near_a) | (__float_as_int(rb) < near_b);
+        mask |= (unsigned)close << u;
+        const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+        const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+        TX = f2_fma(sc, dx, TX);
+        TY = f2_fma(sc, dy, TY);
+        TZ = f2_fma(sc, dz, TZ);
+      }
+      while (mask) {
+        const int u = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int jj = l + (k0 + u) * L;
+        const ulonglong2 xy = sh[jj].xy;
+        const ulonglong2 zl = sh[jj].zl;
         const ulonglong2 yz = sh[jj].yz;
+        f2_t dx = f2_sub(xy.x, HX);
+        f2_t dy = f2_sub(xy.y, HY);
+        f2_t dz = f2_sub(zl.x, HZ);
+        f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+        float ra, rb;
+        f2_unpack(r2, ra, rb);
+        f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+        const f2_t nsc = f2_mul(f2_mul(ri, f2_mul(ri, ri)), f2_pack(-1.f, -1.f));
+        TX = f2_fma(nsc, dx, TX);  // take the hi-only term out again
+        TY = f2_fma(nsc, dy, TY);
+        TZ = f2_fma(nsc, dz, TZ);
         dx = f2_add(dx, f2_sub(zl.y, LX));
         dy = f2_add(dy, f2_sub(yz.x, LY));
         dz = f2_add(dz, f2_sub(yz.y, LZ));
         r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
         f2_unpack(r2, ra, rb);
+        ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+        const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+        TX = f2_fma(sc, dx, TX);
+        TY = f2_fma(sc, dy, TY);
+        TZ = f2_fma(sc, dz, TZ);
       }
-      const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-      const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
-      TX = f2_fma(sc, dx, TX);
-      TY = f2_fma(sc, dy, TY);
-      TZ = f2_fma(sc, dz, TZ);
     }
     float tx[2], ty[2], tz[2];
     f2_unpack(TX, tx[0], tx[1]);

@@ -36,7 +36,7 @@ size_t norm_workspace_bytes(long long n);
 namespace {
 
 template <int PREC, int T, int L, int BPT, bool PACKED = false>
-__global__ void __launch_bounds__(T)
+__global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 1)
     fused_stage_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ FusedParams P, int s) {
   constexpr int BI = (T / L) * BPT;
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(T)
 // repacks the CTA's own tile (centroid, radius, near and far records) for
 // the next stage.
 template <int T, int L, int BPT, bool UNIFORM>
-__global__ void __launch_bounds__(T, 1024 / T)
+__global__ void __launch_bounds__(T, 768 / T)
     fused_sorted_kernel(const __grid_constant__ DevTableau tab,
                         const __grid_constant__ FusedParams P, int s) {
   constexpr int BI = (T / L) * BPT;
