@@ -53,6 +53,7 @@ FLOPS_PER_INTERACTION = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) conven
 # r^-3, 3 FMA accumulations (rsqrt runs on the SFU).  The 20-FLOP convention
 # counts 10 FMA-equivalents, so the FP32 pipe caps the fraction at 10/17.
 HILO_FP32_OPS = 17
+FP64_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (non-tensor), one FMA = 2 FLOP
 
 
 def peaks():
@@ -512,10 +513,15 @@ def run_other_workload(args):
     elif args.workload == "rk_hbm":
         # The standalone element-wise kernels of one RKF78 attempt on vectors of
         # 2^24 doubles (128 MiB each, beyond L2): stage combinations, update and
-        # error, error target, scaled norm.  Algorithmic bytes = every vector
-        # element read or written once; peak = the measured copy bandwidth.
+        # error, error target, scaled norm.  Two ceilings per kernel: HBM
+        # (algorithmic bytes = every vector element read or written once,
+        # against the measured copy bandwidth) and the FP64 pipe (the IEEE
+        # multiply and add per coefficient that bit-for-bit parity needs; a
+        # division counted as ~9 FP64 instructions of a Newton-Raphson
+        # sequence; GB300: 1.25 TFLOP/s = 0.625e12 FP64 instructions/s).
         import ctypes as C
         pk, src = peaks()
+        fp64_ips = FP64_TFLOPS_NOMINAL * 1e12 / 2
         nv = 1 << 24
         t = gb.tableau("RKF78")
         S = t.n_stages
@@ -529,38 +535,49 @@ def run_other_workload(args):
         work = torch.empty(nb, dtype=torch.uint8, device="cuda")
         res_d = torch.zeros(1, dtype=torch.float64, device="cuda")
         sp = gb._stream(stream)
-        nnz_b = sum(1 for j in range(S) if t.b[j] != 0.0 or t.b[j] != t.bt[j])
+        nb_b = sum(1 for j in range(S) if t.b[j] != 0.0)
+        nb_d = sum(1 for j in range(S) if t.b[j] != t.bt[j])
+        nb_u = sum(1 for j in range(S) if t.b[j] != 0.0 or t.b[j] != t.bt[j])
         cases = []
         for s in range(1, S):
             nnz = sum(1 for j in range(s) if t.a[s - 1][j] != 0.0)
-            cases.append((f"rk_stage_{s}", 8 * nv * (nnz + 2),
+            cases.append((f"rk_stage_{s}", 8 * nv * (nnz + 2), nv * (2 * nnz + 2),
                           lambda s=s: gb.rk_stage(t, s, 1e-3, x0, ks, out, nv, stream)))
-        cases.append(("rk_update_state_and_error", 8 * nv * (nnz_b + 3),
+        cases.append(("rk_update_state_and_error", 8 * nv * (nb_u + 3),
+                      nv * (2 * nb_b + 2 * nb_d + 3),
                       lambda: gb.rk_update(t, 1e-3, x0, ks, x, err, nv, stream)))
-        cases.append(("rk_error_target", 8 * nv * 5,
+        cases.append(("rk_error_target", 8 * nv * 5, nv * 2,
                       lambda: gb.rk_error_target(atol, rtol, x, x0, tg, nv, stream)))
-        cases.append(("rk_norm", 8 * nv * 2,
+        cases.append(("rk_norm", 8 * nv * 2, nv * (9 + 2),
                       lambda: gb.check(gb.lib().gb_rk_norm_f64(
                           C.c_void_p(err.data_ptr()), C.c_void_p(tg.data_ptr()), nv,
                           C.c_void_p(work.data_ptr()), nb, C.c_void_p(res_d.data_ptr()), sp),
                           "gb_rk_norm_f64")))
         rows = {}
-        for name, nbytes, fn in cases:
+        for name, nbytes, nops, fn in cases:
             for _ in range(max(args.warmup, 3)):
                 fn()
             ms, _ = _timed(torch, stream, fn, args.steps, flush)
-            gbs = nbytes / (ms / args.steps / 1e3) / 1e9
-            rows[name] = {"bytes": nbytes, "us": 1e3 * ms / args.steps, "GB/s": gbs,
-                          "frac": gbs / pk["hbm_gbs"]}
-        tot_b = sum(r["bytes"] for r in rows.values())
+            sec = ms / args.steps / 1e3
+            hbm = nbytes / sec / 1e9 / pk["hbm_gbs"]
+            f64 = nops / sec / fp64_ips
+            rows[name] = {"bytes": nbytes, "fp64_instr": nops, "us": 1e6 * sec,
+                          "GB/s": nbytes / sec / 1e9, "hbm_frac": hbm, "fp64_frac": f64,
+                          "bound": "fp64" if nops / fp64_ips > nbytes / (pk["hbm_gbs"] * 1e9)
+                          else "hbm"}
         tot_us = sum(r["us"] for r in rows.values())
-        line.update(metric="element-wise RK kernels, achieved HBM bandwidth", unit="GB/s",
-                    value=tot_b / (tot_us / 1e6) / 1e9, dtype="f64", steps=args.steps,
-                    ms_per_step=tot_us / 1e3, kernels=rows,
-                    roofline={"bound": "hbm", "achieved": tot_b / (tot_us / 1e6) / 1e9,
-                              "peak": pk["hbm_gbs"], "unit": "GB/s",
-                              "frac": tot_b / (tot_us / 1e6) / 1e9 / pk["hbm_gbs"],
-                              "peak_source": src},
+        tot_b = sum(r["bytes"] for r in rows.values())
+        tot_o = sum(r["fp64_instr"] for r in rows.values())
+        floor_us = sum(1e6 * max(r["fp64_instr"] / fp64_ips, r["bytes"] / (pk["hbm_gbs"] * 1e9))
+                       for r in rows.values())
+        line.update(metric="element-wise RK kernels of one RKF78 attempt, n_var = 2^24",
+                    unit="GB/s", value=tot_b / (tot_us / 1e6) / 1e9, dtype="f64",
+                    steps=args.steps, ms_per_step=tot_us / 1e3, kernels=rows,
+                    roofline={"bound": "fp64 (stage sums, update, norm) / hbm (target)",
+                              "achieved_us": tot_us, "floor_us": floor_us,
+                              "frac": floor_us / tot_us, "hbm_peak_gbs": pk["hbm_gbs"],
+                              "fp64_peak_instr_per_s": fp64_ips, "peak_source": src,
+                              "fp64_instr": tot_o},
                     config={"workload": "rkf78_elementwise_nvar16777216", "n_var": nv,
                             "tableau": "RKF78", "l2": "flushed (256 MiB write) before each call"})
     else:  # c5a

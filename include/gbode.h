@@ -106,8 +106,10 @@ typedef struct {
   int32_t j_split;       /* CTAs per thread-block cluster sharing one i-tile: 1,2,4,8 (0 = auto) */
   int32_t lanes;         /* lanes per body inside a warp: 1,2,4,8 (0 = auto) */
   int32_t bodies_per_cta;/* i-bodies per CTA: 32..256 (0 = auto) */
-  int32_t reserved;      /* mixed precision: 1 = scalar FP32 path instead of the packed
-                            f32x2 path (two bodies per thread, uniform masses) */
+  int32_t mixed_variant; /* mixed-precision pair loop: 0 = auto, 1 = scalar FP32 (two
+                            bodies per thread), 2 = packed f32x2 with one pair of bodies
+                            per thread, 4 = packed with two pairs; the packed loops need
+                            uniform masses (per-body masses run the scalar loop) */
 } gb_force_tiling;
 
 int gb_nbody_rhs_f64(const double* x_dev, double* dxdt_dev, int64_t n_particles,
@@ -344,7 +346,7 @@ int gb_integrator_destroy(gb_integrator it);
  * on the integrator's stream without the end-of-attempt controller.  The
  * buffers it writes are recomputed by the next attempt. */
 int gb_integrator_launch_stage(gb_integrator it, int32_t stage);
-/* Launch geometry chosen for the fused stage kernel (reserved = threads per
+/* Launch geometry chosen for the fused stage kernel (mixed_variant = the pair loop in use, per
  * CTA) and the number of CTAs per launch. */
 int gb_integrator_geometry(gb_integrator it, gb_force_tiling* out, int64_t* n_ctas);
 /* Dense output (DOPRI5 only, the continuous extension of NumericalRecipes/ */

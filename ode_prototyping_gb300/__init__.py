@@ -50,7 +50,7 @@ class GbTableau(C.Structure):
 
 class GbForceTiling(C.Structure):
     _fields_ = [("j_split", C.c_int32), ("lanes", C.c_int32), ("bodies_per_cta", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("mixed_variant", C.c_int32)]
 
 
 class GbNBodySystem(C.Structure):
@@ -260,9 +260,12 @@ def tableau(name_or_struct) -> GbTableau:
     return t
 
 
-def tiling(j_split=0, lanes=0, bodies_per_cta=0, scalar=False) -> GbForceTiling:
-    """Force-kernel tiling; scalar=True selects the scalar FP32 mixed path."""
-    return GbForceTiling(j_split, lanes, bodies_per_cta, 1 if scalar else 0)
+def tiling(j_split=0, lanes=0, bodies_per_cta=0, scalar=False,
+           mixed_variant=0) -> GbForceTiling:
+    """Force-kernel tiling.  Mixed precision: scalar=True (or mixed_variant=1)
+    selects the scalar FP32 pair loop, mixed_variant=2 / 4 the packed f32x2
+    loop with one / two pairs of bodies per thread, 0 the library's choice."""
+    return GbForceTiling(j_split, lanes, bodies_per_cta, 1 if scalar else mixed_variant)
 
 
 # ----------------------------------------------------------------------------
@@ -597,8 +600,10 @@ class Integrator:
         n = C.c_int64(0)
         check(lib().gb_integrator_geometry(self.h, C.byref(t), C.byref(n)),
               "gb_integrator_geometry")
+        bpt = 4 if t.mixed_variant == 4 else (2 if t.mixed_variant else 1)
         return {"j_split": t.j_split, "lanes": t.lanes, "bodies_per_cta": t.bodies_per_cta,
-                "threads": t.reserved, "ctas": int(n.value)}
+                "threads": t.bodies_per_cta * t.lanes // bpt, "mixed_variant": t.mixed_variant,
+                "ctas": int(n.value)}
 
     def close(self):
         if getattr(self, "h", None):

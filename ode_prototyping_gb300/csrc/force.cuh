@@ -348,34 +348,44 @@ struct __align__(16) PairRec {
   ulonglong2 yz;  // (ly,ly), (lz,lz)
 };
 
-template <int T, int L>
+template <int T, int L, int PB>
 __device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict__ packed,
                                                    long long n, long long i0, long long jb,
                                                    long long je, float eps2, PairRec* sh,
                                                    double (*part)[3]) {
+  // PB pairs of bodies per thread: pair p holds bodies q = 2p and 2p + 1 of
+  // the thread's body group, i.e. i = i0 + q * BG + g.
   constexpr int BG = T / L;
+  constexpr int NB = 2 * PB;
   const int g = threadIdx.x / L;
   const int l = threadIdx.x % L;
-  PackedBody pb[2];
+  f2_t HX[PB], HY[PB], HZ[PB], LX[PB], LY[PB], LZ[PB];
+  int near2[NB];
 #pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    const long long i = i0 + (long long)q * BG + g;
-    if (i < n) {
-      pb[q] = packed[i];
-    } else {
-      pb[q].hw = make_float4(0.f, 0.f, 0.f, 0.f);
-      pb[q].lo = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int p = 0; p < PB; ++p) {
+    PackedBody pb[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const long long i = i0 + (long long)(2 * p + h) * BG + g;
+      if (i < n) {
+        pb[h] = packed[i];
+      } else {
+        pb[h].hw = make_float4(0.f, 0.f, 0.f, 0.f);
+        pb[h].lo = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      near2[2 * p + h] = near_threshold_bits(pb[h].hw.x, pb[h].hw.y, pb[h].hw.z);
     }
+    HX[p] = f2_pack(pb[0].hw.x, pb[1].hw.x);
+    HY[p] = f2_pack(pb[0].hw.y, pb[1].hw.y);
+    HZ[p] = f2_pack(pb[0].hw.z, pb[1].hw.z);
+    LX[p] = f2_pack(pb[0].lo.x, pb[1].lo.x);
+    LY[p] = f2_pack(pb[0].lo.y, pb[1].lo.y);
+    LZ[p] = f2_pack(pb[0].lo.z, pb[1].lo.z);
   }
-  const f2_t HX = f2_pack(pb[0].hw.x, pb[1].hw.x), HY = f2_pack(pb[0].hw.y, pb[1].hw.y),
-             HZ = f2_pack(pb[0].hw.z, pb[1].hw.z);
-  const f2_t LX = f2_pack(pb[0].lo.x, pb[1].lo.x), LY = f2_pack(pb[0].lo.y, pb[1].lo.y),
-             LZ = f2_pack(pb[0].lo.z, pb[1].lo.z);
   const f2_t E2 = f2_pack(eps2, eps2);
-  const int near_a = near_threshold_bits(pb[0].hw.x, pb[0].hw.y, pb[0].hw.z);
-  const int near_b = near_threshold_bits(pb[1].hw.x, pb[1].hw.y, pb[1].hw.z);
-  float sx[2] = {0.f, 0.f}, sy[2] = {0.f, 0.f}, sz[2] = {0.f, 0.f};
-  float cx[2] = {0.f, 0.f}, cy[2] = {0.f, 0.f}, cz[2] = {0.f, 0.f};
+  float sx[NB], sy[NB], sz[NB], cx[NB], cy[NB], cz[NB];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) sx[q] = sy[q] = sz[q] = cx[q] = cy[q] = cz[q] = 0.f;
   constexpr int JT = T;  // bodies per j-tile: one record per thread
   // the next tile's record is loaded into registers while this tile computes
   PackedBody nxt;
@@ -392,7 +402,9 @@ __device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict_
     }
     __syncthreads();
     if (j0 + JT + threadIdx.x < je) nxt = packed[j0 + JT + threadIdx.x];
-    f2_t TX = 0ULL, TY = 0ULL, TZ = 0ULL;  // bit pattern of (+0.f, +0.f)
+    f2_t TX[PB], TY[PB], TZ[PB];
+#pragma unroll
+    for (int p = 0; p < PB; ++p) TX[p] = TY[p] = TZ[p] = 0ULL;  // (+0.f, +0.f)
     // This lane's partners are jj = l + L k, k < kn.  The loop adds every
     // pair's hi-only term without branching and marks close pairs in a
     // 32-bit mask per chunk of 32 k; the marked pairs are then revisited:
@@ -401,24 +413,28 @@ __device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict_
     for (int k0 = 0; k0 < kn; k0 += 32) {
       const int kc = min(32, kn - k0);
       unsigned mask = 0;
-#pragma unroll 4
+#pragma unroll(4 / PB)
       for (int u = 0; u < kc; ++u) {
         const int jj = l + (k0 + u) * L;
         const ulonglong2 xy = sh[jj].xy;
         const f2_t hz = sh[jj].zl.x;
-        const f2_t dx = f2_sub(xy.x, HX);
-        const f2_t dy = f2_sub(xy.y, HY);
-        const f2_t dz = f2_sub(hz, HZ);
-        const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-        float ra, rb;
-        f2_unpack(r2, ra, rb);
-        const bool close = (__float_as_int(ra) < near_a) | (__float_as_int(rb) < near_b);
+        bool close = false;
+#pragma unroll
+        for (int p = 0; p < PB; ++p) {
+          const f2_t dx = f2_sub(xy.x, HX[p]);
+          const f2_t dy = f2_sub(xy.y, HY[p]);
+          const f2_t dz = f2_sub(hz, HZ[p]);
+          const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+          float ra, rb;
+          f2_unpack(r2, ra, rb);
+          close |= (__float_as_int(ra) < near2[2 * p]) | (__float_as_int(rb) < near2[2 * p + 1]);
+          const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+          const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+          TX[p] = f2_fma(sc, dx, TX[p]);
+          TY[p] = f2_fma(sc, dy, TY[p]);
+          TZ[p] = f2_fma(sc, dz, TZ[p]);
+        }
         mask |= (unsigned)close << u;
-        const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-        const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
-        TX = f2_fma(sc, dx, TX);
-        TY = f2_fma(sc, dy, TY);
-        TZ = f2_fma(sc, dz, TZ);
       }
       while (mask) {
         const int u = __ffs(mask) - 1;
@@ -427,42 +443,49 @@ __device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict_
         const ulonglong2 xy = sh[jj].xy;
         const ulonglong2 zl = sh[jj].zl;
         const ulonglong2 yz = sh[jj].yz;
-        f2_t dx = f2_sub(xy.x, HX);
-        f2_t dy = f2_sub(xy.y, HY);
-        f2_t dz = f2_sub(zl.x, HZ);
-        f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-        float ra, rb;
-        f2_unpack(r2, ra, rb);
-        f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-        const f2_t nsc = f2_mul(f2_mul(ri, f2_mul(ri, ri)), f2_pack(-1.f, -1.f));
-        TX = f2_fma(nsc, dx, TX);  // take the hi-only term out again
-        TY = f2_fma(nsc, dy, TY);
-        TZ = f2_fma(nsc, dz, TZ);
-        dx = f2_add(dx, f2_sub(zl.y, LX));
-        dy = f2_add(dy, f2_sub(yz.x, LY));
-        dz = f2_add(dz, f2_sub(yz.y, LZ));
-        r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-        f2_unpack(r2, ra, rb);
-        ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-        const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
-        TX = f2_fma(sc, dx, TX);
-        TY = f2_fma(sc, dy, TY);
-        TZ = f2_fma(sc, dz, TZ);
+#pragma unroll
+        for (int p = 0; p < PB; ++p) {
+          f2_t dx = f2_sub(xy.x, HX[p]);
+          f2_t dy = f2_sub(xy.y, HY[p]);
+          f2_t dz = f2_sub(zl.x, HZ[p]);
+          f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+          float ra, rb;
+          f2_unpack(r2, ra, rb);
+          f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+          const f2_t nsc = f2_mul(f2_mul(ri, f2_mul(ri, ri)), f2_pack(-1.f, -1.f));
+          TX[p] = f2_fma(nsc, dx, TX[p]);  // take the hi-only term out again
+          TY[p] = f2_fma(nsc, dy, TY[p]);
+          TZ[p] = f2_fma(nsc, dz, TZ[p]);
+          dx = f2_add(dx, f2_sub(zl.y, LX[p]));
+          dy = f2_add(dy, f2_sub(yz.x, LY[p]));
+          dz = f2_add(dz, f2_sub(yz.y, LZ[p]));
+          r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+          f2_unpack(r2, ra, rb);
+          ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+          const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+          TX[p] = f2_fma(sc, dx, TX[p]);
+          TY[p] = f2_fma(sc, dy, TY[p]);
+          TZ[p] = f2_fma(sc, dz, TZ[p]);
+        }
       }
     }
-    float tx[2], ty[2], tz[2];
-    f2_unpack(TX, tx[0], tx[1]);
-    f2_unpack(TY, ty[0], ty[1]);
-    f2_unpack(TZ, tz[0], tz[1]);
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      kahan_add(sx[q], cx[q], tx[q]);
-      kahan_add(sy[q], cy[q], ty[q]);
-      kahan_add(sz[q], cz[q], tz[q]);
+    for (int p = 0; p < PB; ++p) {
+      float tx[2], ty[2], tz[2];
+      f2_unpack(TX[p], tx[0], tx[1]);
+      f2_unpack(TY[p], ty[0], ty[1]);
+      f2_unpack(TZ[p], tz[0], tz[1]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = 2 * p + h;
+        kahan_add(sx[q], cx[q], tx[h]);
+        kahan_add(sy[q], cy[q], ty[h]);
+        kahan_add(sz[q], cz[q], tz[h]);
+      }
     }
   }
 #pragma unroll
-  for (int q = 0; q < 2; ++q) {
+  for (int q = 0; q < NB; ++q) {
     double ax = dsub((double)sx[q], (double)cx[q]);
     double ay = dsub((double)sy[q], (double)cy[q]);
     double az = dsub((double)sz[q], (double)cz[q]);
@@ -637,16 +660,22 @@ __device__ __forceinline__ PackedBody pack_body(double x, double y, double z, do
 }
 
 // Launch geometry shared by the standalone and fused kernels.
+// Mixed pair loop used when the tiling leaves the choice open (1 scalar,
+// 2 / 4 packed with one / two pairs of bodies per thread).
+constexpr int kDefaultMixedVariant = 2;
+
 struct ForceGeom {
   int T;      // threads per CTA
   int L;      // lanes per body
   int P;      // cluster size
   int BPT;    // bodies per thread (mixed path)
+  int variant;  // mixed pair loop: 1 scalar, 2 / 4 packed with 1 / 2 pairs per thread
   long long n_itiles;
   int bodies_per_cta() const { return (T / L) * BPT; }
 };
 
-ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling, int exact);
+ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling, int exact,
+                      bool uniform_masses = true);
 int launch_cluster(const void* kernel, const ForceGeom& g, size_t smem, cudaStream_t s,
                    void** args);
 

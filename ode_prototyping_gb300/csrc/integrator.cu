@@ -36,7 +36,7 @@ size_t norm_workspace_bytes(long long n);
 namespace {
 
 template <int PREC, int T, int L, int BPT, bool PACKED = false>
-__global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 1)
+__global__ void __launch_bounds__(T, PACKED && BPT == 2 ? 7 * 128 / T : (PACKED ? 4 * 128 / T : 1))
     fused_stage_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ FusedParams P, int s) {
   constexpr int BI = (T / L) * BPT;
@@ -70,8 +70,8 @@ __global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 1)
     } else {
       const PackedBody* src = (s == 0) ? P.PX + (long long)px * n : P.PY + (long long)(s & 1) * n;
       if constexpr (PACKED) {
-        force_mixed_cta_x2<T, L>(src, n, i0, jb, je, P.eps2f,
-                                 reinterpret_cast<PairRec*>(sh_raw), part);
+        force_mixed_cta_x2<T, L, BPT / 2>(src, n, i0, jb, je, P.eps2f,
+                                          reinterpret_cast<PairRec*>(sh_raw), part);
       } else if (P.masses) {
         force_mixed_cta<T, L, BPT, false>(src, n, i0, jb, je, P.eps2f,
                                           reinterpret_cast<PackedBody*>(sh_raw), part);
@@ -476,20 +476,21 @@ const void* pick_L(int L) {
   }
 }
 
-template <int T>
+template <int T, int BPT>
 const void* pick_packed(int L) {
   switch (L) {
-    case 1: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 1, 2, true>;
-    case 2: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 2, 2, true>;
-    case 4: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 4, 2, true>;
+    case 1: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 1, BPT, true>;
+    case 2: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 2, BPT, true>;
+    case 4: return (const void*)fused_stage_kernel<GB_PREC_MIXED, T, 4, BPT, true>;
     default: return nullptr;
   }
 }
 
 const void* pick_fused(int prec, int T, int L, int BPT, bool packed = false) {
-  if (prec == GB_PREC_MIXED && packed && BPT == 2) {
-    if (T == 128) return pick_packed<128>(L);
-    if (T == 256) return pick_packed<256>(L);
+  if (prec == GB_PREC_MIXED && packed) {
+    if (T == 128 && BPT == 2) return pick_packed<128, 2>(L);
+    if (T == 128 && BPT == 4) return pick_packed<128, 4>(L);
+    if (T == 256 && BPT == 2) return pick_packed<256, 2>(L);
     return nullptr;
   }
   if (prec == GB_PREC_F64) {
@@ -759,7 +760,8 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   it->A = opts.attempts_per_sync;
   it->R = opts.record ? it->A + 2 : 2;
   it->user_stream = as_cuda(stream);
-  it->geom = choose_geom(it->n, opts.precision, &opts.tiling, opts.exact);
+  it->geom = choose_geom(it->n, opts.precision, &opts.tiling, opts.exact,
+                         sys->masses_dev == nullptr);
   if (opts.precision == GB_PREC_F64) it->geom.BPT = 1;
   if (opts.precision == GB_PREC_MIXED && it->geom.T < 128) it->geom.T = 128;
   // spatially sorted tiles (mixed precision): on unless switched off
@@ -771,7 +773,7 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   it->geom.n_itiles = (it->n + it->geom.bodies_per_cta() - 1) / it->geom.bodies_per_cta();
   it->kernel = it->sorted ? pick_sorted(it->geom.T, it->geom.L, sys->masses_dev == nullptr)
                           : pick_fused(opts.precision, it->geom.T, it->geom.L, it->geom.BPT,
-                                       sys->masses_dev == nullptr && opts.tiling.reserved != 1);
+                                       it->geom.variant != 1);
   int rc = GB_OK;
   auto fail = [&](int code) {
     free_all(it);
@@ -1078,7 +1080,7 @@ extern "C" int gb_integrator_geometry(gb_integrator it, gb_force_tiling* out, in
   out->j_split = it->geom.P;
   out->lanes = it->geom.L;
   out->bodies_per_cta = it->geom.bodies_per_cta();
-  out->reserved = it->geom.T;
+  out->mixed_variant = it->geom.variant;
   if (n_ctas) *n_ctas = it->geom.n_itiles * it->geom.P;
   return GB_OK;
 }

@@ -97,9 +97,9 @@ __global__ void __launch_bounds__(T) rhs_mixed_kernel(const PackedBody* __restri
   long long jb, je;
   j_chunk(n, ci.rank, ci.size, T, jb, je);
   if constexpr (PACKED) {
-    static_assert(BPT == 2, "packed path carries two bodies per thread");
-    force_mixed_cta_x2<T, L>(packed, n, i0, jb, je, eps2, reinterpret_cast<PairRec*>(sh_raw),
-                             part);
+    static_assert(BPT == 2 || BPT == 4, "packed path carries one or two pairs per thread");
+    force_mixed_cta_x2<T, L, BPT / 2>(packed, n, i0, jb, je, eps2,
+                                      reinterpret_cast<PairRec*>(sh_raw), part);
   } else {
     PackedBody* sh = reinterpret_cast<PackedBody*>(sh_raw);
     if (uniform_mass)
@@ -141,10 +141,11 @@ const void* pick_mixed_L(int L) {
   }
 }
 
-// packed: the f32x2 path (two bodies per thread, uniform masses)
+// packed: the f32x2 path (pairs of bodies per thread, uniform masses)
 template <int T>
 const void* pick_mixed(int L, int BPT, bool packed = false) {
   if (packed && BPT == 2) return pick_mixed_L<T, 2, true>(L);
+  if (packed && BPT == 4) return pick_mixed_L<T, 4, true>(L);
   switch (BPT) {
     case 1: return pick_mixed_L<T, 1, false>(L);
     case 2: return pick_mixed_L<T, 2, false>(L);
@@ -153,10 +154,10 @@ const void* pick_mixed(int L, int BPT, bool packed = false) {
   }
 }
 
-// The packed path is used for uniform masses with two bodies per thread
-// unless the tiling asks for the scalar path (reserved == 1).
+// The packed loops run for uniform masses unless the tiling asks for the
+// scalar loop (mixed_variant == 1).
 bool use_packed(const gb_force_tiling* tiling, int BPT, const double* masses) {
-  return BPT == 2 && !masses && !(tiling && tiling->reserved == 1);
+  return (BPT == 2 || BPT == 4) && !masses && !(tiling && tiling->mixed_variant == 1);
 }
 
 int validate_nbody(const void* a, const void* b, long long n, double softening, double mass,
@@ -201,7 +202,7 @@ int rhs_for_start(int prec, const double* x, double* dxdt, long long n, double s
     return run_f64(x, x + 3 * n, dxdt, dxdt + 3 * n, n, softening, mass, masses, kModeRhs, &t,
                    s);
   }
-  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
+  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0, masses == nullptr);
   const void* k = nullptr;
   switch (g.T) {
     case 64: k = pick_mixed<64>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
@@ -240,12 +241,14 @@ int launch_cluster(const void* kernel, const ForceGeom& g, size_t smem, cudaStre
   return GB_OK;
 }
 
-ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling, int exact) {
+ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling, int exact,
+                      bool uniform_masses) {
   ForceGeom g;
   g.T = 128;
   g.L = 1;
   g.P = 1;
   g.BPT = 1;
+  g.variant = 0;
   const int sms = num_sms();
   if (exact) {
     g.L = 1;
@@ -261,7 +264,11 @@ ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling,
     g.P = P;
     g.L = L;
   } else {
-    g.BPT = 2;
+    int v = tiling ? tiling->mixed_variant : 0;
+    if (v != 1 && v != 2 && v != 4) v = kDefaultMixedVariant;
+    if (!uniform_masses) v = 1;
+    g.variant = v;
+    g.BPT = v == 4 ? 4 : 2;
     // ~16 warps per SM, each lane pair-loop at least ~256 partners long.
     long long want = (long long)sms * 16 * 32 * g.BPT;
     long long lp = (want + n - 1) / n;
@@ -317,7 +324,7 @@ int mixed_rhs_into(const double* x, double* dxdt, long long n, double softening,
   GB_CUDA_TRY(cudaGetLastError());
   pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, masses, c, n, packed);
   GB_CUDA_TRY(cudaGetLastError());
-  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
+  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0, masses == nullptr);
   const void* k = nullptr;
   switch (g.T) {
     case 64: k = pick_mixed<64>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
@@ -430,7 +437,7 @@ extern "C" int gb_nbody_rhs_mixed_sorted(const double* x, double* dxdt, int64_t 
   const long long nt = (n + 127) / 128;
   GB_TRY(sort_and_pack(x, nullptr, 0, n, w.sb, masses, w.cref, w.near, w.far, w.meta, nullptr,
                        nt, 128, s));
-  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
+  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0, masses == nullptr);
   g.T = 128;
   if (g.L > 2) g.L = 2;
   g.BPT = g.L;
@@ -472,7 +479,7 @@ extern "C" int gb_nbody_rhs_mixed(const double* x, double* dxdt, int64_t n, doub
   GB_CUDA_TRY(cudaGetLastError());
   pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, masses, c, n, packed);
   GB_CUDA_TRY(cudaGetLastError());
-  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0);
+  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0, masses == nullptr);
   const void* k = nullptr;
   switch (g.T) {
     case 64: k = pick_mixed<64>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;

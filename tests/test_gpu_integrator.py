@@ -115,12 +115,16 @@ def test_vector_tolerances_match_scalar(gb, torch_cuda):
     np.testing.assert_array_equal(np.array(o1.states()), np.array(o2.states()))
 
 
-def test_mixed_precision_integrator(gb, torch_cuda):
+@pytest.mark.parametrize("variant", [0, 1, 2, 4])
+def test_mixed_precision_integrator(gb, torch_cuda, variant):
+    """Every mixed pair loop (auto, scalar, one or two packed pairs per
+    thread) tracks the FP64 path."""
     n = 1024
     x0 = gb.ic_uniform_ball(n, 1, 0.1)
     tol = 1e-9
     t64, s64, st64 = run(gb, "DOPRI5", n, 0.01, 1.0 / n, x0, 0.0, 0.1, tol)
-    tmx, smx, stmx = run(gb, "DOPRI5", n, 0.01, 1.0 / n, x0, 0.0, 0.1, tol, precision="mixed")
+    tmx, smx, stmx = run(gb, "DOPRI5", n, 0.01, 1.0 / n, x0, 0.0, 0.1, tol, precision="mixed",
+                         tile=gb.tiling(mixed_variant=variant))
     assert abs(len(tmx) - len(t64)) <= max(2, len(t64) // 20)
     assert np.max(np.abs(smx[-1] - s64[-1])) <= 1e-6
 

@@ -89,17 +89,24 @@ def test_acc_write_and_accumulate(gb, orc, torch_cuda):
     np.testing.assert_array_equal(acc.cpu().numpy(), 2 * ref)
 
 
+@pytest.mark.parametrize("variant", [0, 1, 4])
 @pytest.mark.parametrize("n,soft,gen", [(1024, 0.01, "ball"), (4096, 0.005, "plummer"),
-                                        (16384, 0.005, "plummer"), (3001, 0.003, "binary")])
-def test_rhs_mixed_within_1e6_of_fp64(gb, torch_cuda, n, soft, gen):
+                                        (16384, 0.005, "plummer"), (3001, 0.003, "binary"),
+                                        (8192, 0.002, "cold")])
+def test_rhs_mixed_within_1e6_of_fp64(gb, torch_cuda, n, soft, gen, variant):
+    """Hi-only pair differences with hi/lo for close pairs, every pair loop:
+    accelerations within 1e-6 of FP64 (normwise and for the median body)."""
     if gen == "ball":
         x = gb.ic_uniform_ball(n, 1, 0.1)
     elif gen == "plummer":
         x = gb.ic_plummer(n, 2)
+    elif gen == "cold":
+        x = gb.ic_cold_sphere(n, 4, 0.01)
     else:
         x = gb.ic_binary_plummer(n, 3, 0.1, 1e-3, 1e-2)
     ref = gb.nbody_rhs_f64(x, n, soft, 1.0 / n).cpu().numpy()
-    got = gb.nbody_rhs_mixed(x, n, soft, 1.0 / n).cpu().numpy()
+    got = gb.nbody_rhs_mixed(x, n, soft, 1.0 / n,
+                             tile=gb.tiling(mixed_variant=variant)).cpu().numpy()
     np.testing.assert_array_equal(got[: 3 * n], ref[: 3 * n])
     a_g, a_r = got[3 * n:].reshape(-1, 3), ref[3 * n:].reshape(-1, 3)
     # normwise relative error of the acceleration field
