@@ -119,7 +119,8 @@ def load_mlp(args):
     if args.controller != "learned":
         return None
     import ode_prototyping_gb300 as gb
-    path = args.mlp or os.path.join(ROOT, "ode_prototyping_gb300", "weights", "proposer_rkf78.bin")
+    path = args.mlp or os.path.join(ROOT, "ode_prototyping_gb300", "weights",
+                                   "proposer_plummer16384_rkf78.bin")
     return gb.GbMlp.from_buffer_copy(open(path, "rb").read())
 
 
@@ -228,8 +229,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--controller", default="reference", choices=["reference", "pi", "learned"])
     ap.add_argument("--mlp", default=None, help="trained proposer weights (learned controller)")
+    ap.add_argument("--learned-config", default="plummer4096_rkf78",
+                    help="c4: proposer training/evaluation configuration")
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c2_f64", "c1", "c3", "c5a", "c5b", "rk_hbm"],
+                    choices=["c2", "c2_f64", "c1", "c3", "c4", "c5a", "c5b", "rk_hbm"],
                     help="c2 (default, the headline), or another configuration")
     args = ap.parse_args()
     world, rank, local = dist_setup()
@@ -510,6 +513,27 @@ def run_other_workload(args):
                             "n_min": int(sizes.min()), "n_max": int(sizes.max()),
                             "bodies": int(sizes.sum()), "tableau": tab, "atol": tol,
                             "rtol": tol, "t": [0, tf], "step": "whole batch integration"})
+    elif args.workload == "c4":
+        # Learned step-size proposer: trained on seed set A (weights shipped in
+        # ode_prototyping_gb300/weights/, retrained here if absent), evaluated
+        # on held-out seed set B against the reference and PI controllers.
+        from ode_prototyping_gb300 import learned
+        cfg = args.learned_config
+        path = os.path.join(ROOT, "ode_prototyping_gb300", "weights", f"proposer_{cfg}.bin")
+        trained_here = not os.path.exists(path)
+        if trained_here:
+            m, _ = learned.train_config(cfg)
+        else:
+            m = gb.GbMlp.from_buffer_copy(open(path, "rb").read())
+        ev = learned.evaluate_config(cfg, m)
+        c = learned.CONFIGS[cfg]
+        lrn = ev["learned"]
+        line.update(value=lrn["accepted"] / lrn["wall_s"], dtype="f32+f64", steps=1,
+                    ms_per_step=1e3 * lrn["wall_s"], controllers=ev,
+                    config={"workload": f"learned_proposer_{cfg}", **c,
+                            "train_seeds": "A = 1..8", "eval_seeds": "B = 101..104",
+                            "weights": "trained in this run" if trained_here else path[len(ROOT) + 1:],
+                            "step": "whole integrations of the held-out systems"})
     elif args.workload == "rk_hbm":
         # The standalone element-wise kernels of one RKF78 attempt on vectors of
         # 2^24 doubles (128 MiB each, beyond L2): stage combinations, update and

@@ -179,3 +179,70 @@ def evaluate(n, softening, tab, tol, t_end, seeds, mlp, precision="mixed", ic="p
         agg["states"] = [r["state"] for r in rows]
         out[ctl] = agg
     return out
+
+
+# Workloads the proposer is trained and evaluated on (seed set A trains,
+# seed set B evaluates).
+CONFIGS = {
+    # N = 16384 Plummer sphere, RKF78, tol 1e-8 (the single large system)
+    "plummer16384_rkf78": dict(ic="plummer", n=16384, softening=0.005, tab="RKF78", tol=1e-8,
+                               tf=2.0, attempts=400),
+    # the same family at N = 4096 over t in [0, 0.5] (quick to train)
+    "plummer4096_rkf78": dict(ic="plummer", n=4096, softening=0.005, tab="RKF78", tol=1e-8,
+                              tf=0.5, attempts=300),
+    # binary-rich Plummer spheres, DOPRI5, tol 1e-8
+    "binary2048_dopri5": dict(ic="binary", n=2048, softening=1e-4, tab="DOPRI5", tol=1e-8,
+                              tf=0.02, attempts=300),
+}
+SEEDS_A = list(range(1, 17))
+SEEDS_B = list(range(101, 117))
+
+
+def train_config(name: str, seeds=None, rounds: int = 3, rho: float = 0.6, epochs: int = 3000):
+    c = CONFIGS[name]
+    return fit(seeds or SEEDS_A[:8], c["n"], c["softening"], c["tab"], c["tol"], c["tf"],
+               c["attempts"], rounds=rounds, rho=rho, epochs=epochs, ic=c["ic"])
+
+
+def evaluate_config(name: str, mlp: GbMlp, seeds=None) -> dict:
+    """Reference, PI and learned controllers on held-out seeds, plus the
+    learned run's gain over the reference controller."""
+    c = CONFIGS[name]
+    ev = evaluate(c["n"], c["softening"], c["tab"], c["tol"], c["tf"], seeds or SEEDS_B[:4], mlp,
+                  ic=c["ic"])
+    states = {k: v.pop("states") for k, v in ev.items()}
+    ref, lrn = ev["reference"], ev["learned"]
+    ev["gain"] = {
+        "rhs_saved_fraction": 1.0 - lrn["rhs"] / ref["rhs"],
+        "rejected_fraction_reference": ref["rejected_fraction"],
+        "rejected_fraction_learned": lrn["rejected_fraction"],
+        "energy_err_ratio": lrn["energy_rel_err_max"] / max(ref["energy_rel_err_max"], 1e-300),
+        "wall_speedup": ref["wall_s"] / lrn["wall_s"],
+        "max_state_diff_vs_reference": max(float((a - b).abs().max().item())
+                                           for a, b in zip(states["learned"],
+                                                           states["reference"])),
+    }
+    return ev
+
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="train the learned step-size proposer")
+    ap.add_argument("--config", default="plummer16384_rkf78", choices=sorted(CONFIGS))
+    ap.add_argument("--out", required=True, help="weights file (raw gb_mlp)")
+    ap.add_argument("--rho", type=float, default=0.6)
+    ap.add_argument("--rounds", type=int, default=3)
+    ap.add_argument("--seeds", type=int, default=8, help="seeds 1..k of seed set A")
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    m, info = train_config(a.config, SEEDS_A[:a.seeds], rounds=a.rounds, rho=a.rho)
+    with open(a.out, "wb") as f:
+        f.write(bytes(m))
+    ev = evaluate_config(a.config, m)
+    print(json.dumps({"config": a.config, "train": info, "train_s": time.time() - t0,
+                      "evaluation": ev}, indent=1))
+
+
+if __name__ == "__main__":
+    main()
