@@ -128,11 +128,13 @@ __device__ inline void finish_attempt(const DevTableau& tab, const CtrlEnv& P, C
     dtn = pi_step(c, dt, err, accepted);
   } else if (c.controller == GB_CTRL_LEARNED) {
     if (accepted && have_learned) {
-      // The network proposes a correction to the elementary controller's
-      // log step ratio log(safety) - log(err) / (1 + q); the embedded error
+      // The network proposes a correction to the PI controller's log step
+      // ratio log(safety) - alpha log(err) + beta log(err_prev) (a network
+      // that has learned nothing reproduces PI); the embedded error
       // estimate of the next attempt still decides acceptance.
-      const double base =
-          err > 0.0 ? log(c.safety) - log(err) / (1.0 + c.q) : log(kMaxStepScale);
+      const double base = err > 0.0 ? log(c.safety) - c.pi_alpha * log(err) +
+                                          c.pi_beta * log(c.err_prev)
+                                    : log(kMaxStepScale);
       const double lg = fmin(fmax(base + learned_log_scale, log(kMinStepScale)),
                              log(kMaxStepScale));
       double scale = exp(lg);

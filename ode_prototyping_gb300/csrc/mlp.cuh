@@ -55,7 +55,8 @@ __device__ __forceinline__ void make_features(const Ctrl& c, const DevTableau& t
   f[10] = (float)log(fmax(c.dt_hist[0] / fmax(c.tf - c.t0, tiny), tiny));
   f[11] = (float)c.last_accepted;
   f[12] = (float)(log(fmax(c.dt_hist[0], tiny)) - log(fmax(c.dt_hist[1], tiny)));
-  f[13] = f[14] = f[15] = 0.f;
+  f[13] = (float)log(fmax(c.err_prev, 1e-30));  // PI memory: last accepted error
+  f[14] = f[15] = 0.f;
 }
 
 // Single-thread BF16-weight / FP32-accumulate forward pass.

@@ -59,14 +59,21 @@ def collect_logs(seeds, n: int, softening: float, tab: str, tol: float, tf: floa
     return logs
 
 
-def build_dataset(logs, q: int, rho: float = 0.6):
+PI_BETA = 0.04  # the integrator's default PI memory exponent
+
+
+def build_dataset(logs, q: int, rho: float = 0.6, pi_beta: float = PI_BETA):
+    """Targets are residuals over the PI controller's log step ratio
+    log(safety) - alpha log(err_k) + beta log(err_prev) (feature 13 holds
+    log(err_prev)), the base the device adds the network output to."""
     xs, ys = [], []
     log_safety = np.log(0.38) / (1.0 + q)
+    alpha = 1.0 / (1.0 + q) - 0.75 * pi_beta
     for rec in logs:
         for k in range(len(rec) - 1):
             if rec[k, ACCEPTED] < 0.5:
                 continue
-            base = log_safety - rec[k, LOG_ERR] / (q + 1)
+            base = log_safety - alpha * rec[k, LOG_ERR] + pi_beta * rec[k, 13]
             target = (rec[k + 1, LOG_DT] + (np.log(rho) - rec[k + 1, LOG_ERR]) / (q + 1)
                       - rec[k, LOG_DT] - base)
             if not np.isfinite(target):
@@ -89,9 +96,36 @@ def _from_device_struct(buf) -> GbMlp:
     return GbMlp.from_buffer_copy(raw)
 
 
+def _val_loss(m: GbMlp, x: np.ndarray, y: np.ndarray, over_weight: float) -> float:
+    """Mean asymmetric squared error of the FP32 forward pass (library kernel)."""
+    import torch
+    w = _to_device_struct(m)
+    xd = torch.as_tensor(np.ascontiguousarray(x), device="cuda")
+    yd = torch.empty(len(y), dtype=torch.float32, device="cuda")
+    check(lib().gb_mlp_forward_f32(w.data_ptr(), xd.data_ptr(), yd.data_ptr(), len(y), None,
+                                   None), "gb_mlp_forward_f32")
+    d = yd.cpu().numpy() - y
+    return float(np.mean(np.where(d > 0, over_weight, 1.0) * d * d))
+
+
 def train(x: np.ndarray, y: np.ndarray, epochs: int = 3000, lr: float = 3e-3,
-          over_weight: float = 3.0, seed: int = 0):
-    """Returns (trained gb_mlp in host memory, final loss)."""
+          over_weight: float = 3.0, seed: int = 0, val_frac: float = 0.0,
+          epoch_grid=(100, 300, 1000, 3000)):
+    """Returns (trained gb_mlp in host memory, final loss).  With val_frac > 0
+    a seeded random share of the samples is held out and the training length
+    is chosen from epoch_grid by the held-out loss (early stopping)."""
+    if val_frac > 0.0:
+        rng = np.random.default_rng(seed + 1)
+        perm = rng.permutation(len(y))
+        nv = max(1, int(len(y) * val_frac))
+        vi, ti = perm[:nv], perm[nv:]
+        best = None
+        for e in epoch_grid:
+            m, _ = train(x[ti], y[ti], epochs=e, lr=lr, over_weight=over_weight, seed=seed)
+            v = _val_loss(m, x[vi], y[vi], over_weight)
+            if best is None or v < best[0]:
+                best = (v, m)
+        return best[1], best[0]
     import torch
     m = GbMlp()
     check(lib().gb_mlp_init(C.byref(m), seed), "gb_mlp_init")
@@ -130,8 +164,8 @@ def fit(seeds, n: int, softening: float, tab: str, tol: float, tf: float, attemp
             logs += collect_logs(seeds, n, softening, tab, tol, tf, attempts,
                                  controller="learned", mlp=m, ic=ic)
         x, y = build_dataset(logs, q, rho)
-        m, loss = train(x, y, epochs=epochs, over_weight=over_weight)
-        info.append({"round": r, "samples": int(len(y)), "loss": loss})
+        m, loss = train(x, y, epochs=epochs, over_weight=over_weight, val_frac=0.2)
+        info.append({"round": r, "samples": int(len(y)), "val_loss": loss})
     return m, info
 
 
