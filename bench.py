@@ -126,6 +126,25 @@ def load_mlp(args):
     return gb.GbMlp.from_buffer_copy(open(path, "rb").read())
 
 
+def aggregate_over_ranks(accepted: float, rhs: float, ms: float, device: str = "cuda"):
+    """Whole-job totals over replicas (one independent system per GPU):
+    accepted steps and RHS evaluations summed, device time = max over ranks."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized() or dist.get_world_size() == 1:
+        return accepted, rhs, ms
+    tt = torch.tensor([accepted, rhs], dtype=torch.float64, device=device)
+    dist.all_reduce(tt)
+    tm = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+    return float(tt[0]), float(tt[1]), float(tm[0])
+
+
+def replica_seed(rank: int) -> int:
+    """Seed of the system rank `rank` integrates (replicas are independent)."""
+    return WORKLOAD["seed"] + rank
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -254,7 +273,7 @@ def main():
     W = WORKLOAD
     n = W["n_particles"]
     eps = W["softening"]
-    seed = W["seed"] + rank  # replicas: an independent system per GPU
+    seed = replica_seed(rank)  # replicas: an independent system per GPU
     x0 = gb.ic_plummer(n, seed, 1.0)
     stream = torch.cuda.Stream()
     ode = gb.NBodyODE(n, eps, 1.0 / n)
@@ -308,14 +327,7 @@ def main():
     replays = -(-per_job["attempts"] // A)
     launches_per_job = 12 + replays * A * (S + 1)
     # whole-job aggregate over ranks: accepted steps summed, time = max
-    acc_all, ms_max, rhs_all = float(accepted), ms, float(rhs)
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([acc_all, rhs_all], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt)
-        tm = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        acc_all, rhs_all, ms_max = float(tt[0]), float(tt[1]), float(tm[0])
+    acc_all, rhs_all, ms_max = aggregate_over_ranks(float(accepted), float(rhs), ms)
     value = acc_all / (ms_max / 1e3)
     pair_rate = rhs_all * n * (n - 1) / (ms_max / 1e3)
 

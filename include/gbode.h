@@ -103,7 +103,8 @@ int gb_pointer_kind(const void* ptr);
 /* executor bit for bit; 0 lets the library choose.                        */
 /* ---------------------------------------------------------------------- */
 typedef struct {
-  int32_t j_split;       /* CTAs per thread-block cluster sharing one i-tile: 1,2,4,8 (0 = auto) */
+  int32_t j_split;       /* CTAs per thread-block cluster sharing one i-tile: 1,2,4,8,16
+                            (0 = auto; 16 is a non-portable cluster size) */
   int32_t lanes;         /* lanes per body inside a warp: 1,2,4,8 (0 = auto) */
   int32_t bodies_per_cta;/* i-bodies per CTA: 32..256 (0 = auto) */
   int32_t mixed_variant; /* mixed-precision pair loop: 0 = auto, 1 = scalar FP32 (two

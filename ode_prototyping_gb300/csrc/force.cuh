@@ -413,7 +413,7 @@ __device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict_
     for (int k0 = 0; k0 < kn; k0 += 32) {
       const int kc = min(32, kn - k0);
       unsigned mask = 0;
-#pragma unroll(8 / PB)
+#pragma unroll(4 / PB)
       for (int u = 0; u < kc; ++u) {
         const int jj = l + (k0 + u) * L;
         const ulonglong2 xy = sh[jj].xy;

@@ -781,6 +781,10 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
     return code;
   };
   if (!it->kernel) return fail(GB_ERR_UNSUPPORTED);
+  if (it->geom.P > 8 &&
+      cudaFuncSetAttribute(it->kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+          cudaSuccess)
+    return fail(GB_ERR_UNSUPPORTED);  // 16-CTA clusters opt-in before any graph capture
   const long long n = it->n, nv = it->n_var;
   cudaError_t e = cudaSuccess;
 #define GB_ALLOC(ptr, bytes)                                        \

@@ -235,7 +235,13 @@ int launch_cluster(const void* kernel, const ForceGeom& g, size_t smem, cudaStre
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (g.P > 8) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    // clusters above 8 CTAs are opt-in per kernel; the attribute is set on
+    // the first (uncaptured) launch and persists
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    GB_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusNone)
+      GB_CUDA_TRY(
+          cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   }
   GB_CUDA_TRY(cudaLaunchKernelExC(&cfg, kernel, args));
   return GB_OK;

@@ -232,7 +232,7 @@ SEEDS_A = list(range(1, 17))
 SEEDS_B = list(range(101, 117))
 
 
-def train_config(name: str, seeds=None, rounds: int = 3, rho: float = 0.6, epochs: int = 3000):
+def train_config(name: str, seeds=None, rounds: int = 3, rho: float = 0.38, epochs: int = 3000):
     c = CONFIGS[name]
     return fit(seeds or SEEDS_A[:8], c["n"], c["softening"], c["tab"], c["tol"], c["tf"],
                c["attempts"], rounds=rounds, rho=rho, epochs=epochs, ic=c["ic"])
@@ -265,7 +265,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description="train the learned step-size proposer")
     ap.add_argument("--config", default="plummer16384_rkf78", choices=sorted(CONFIGS))
     ap.add_argument("--out", required=True, help="weights file (raw gb_mlp)")
-    ap.add_argument("--rho", type=float, default=0.6)
+    ap.add_argument("--rho", type=float, default=0.38)
     ap.add_argument("--rounds", type=int, default=3)
     ap.add_argument("--seeds", type=int, default=8, help="seeds 1..k of seed set A")
     a = ap.parse_args(argv)

@@ -1,0 +1,65 @@
+"""Host logic of the multi-GPU path (replicas only: one independent system
+per GPU, no data-path collective) on CPU: two gloo ranks aggregate their
+per-rank results the way bench.py does (sums of work, max of time), each
+rank integrates a different seed, and the reference arm runs on rank 0 only."""
+import os
+import socket
+import sys
+
+import pytest
+import torch.multiprocessing as mp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world))
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    acc, rhs, ms = bench.aggregate_over_ranks(100.0 + rank, 1000.0 * (rank + 1), 5.0 + 3.0 * rank,
+                                              device="cpu")
+    q.put((rank, acc, rhs, ms, bench.replica_seed(rank)))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_aggregation_gloo():
+    world, port = 2, _free_port()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank_main, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    out = [q.get(timeout=120) for _ in range(world)]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    seeds = set()
+    for rank, acc, rhs, ms, seed in out:
+        assert acc == 201.0 and rhs == 3000.0 and ms == 8.0  # sum, sum, max over ranks
+        seeds.add(seed)
+    assert len(seeds) == world  # an independent system per rank
+
+
+def test_single_process_aggregation_is_identity():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.aggregate_over_ranks(7.0, 8.0, 9.0, device="cpu") == (7.0, 8.0, 9.0)
+
+
+def test_reference_arm_runs_on_rank_zero_only(capsys):
+    sys.path.insert(0, ROOT)
+    import argparse
+    import bench
+    args = argparse.Namespace(gpus=2, steps=1, warmup=0)
+    assert bench.run_reference(args, world=2, rank=1) is None  # returns without work
+    assert capsys.readouterr().out == ""
