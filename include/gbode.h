@@ -109,8 +109,10 @@ typedef struct {
   int32_t bodies_per_cta;/* i-bodies per CTA: 32..256 (0 = auto) */
   int32_t mixed_variant; /* mixed-precision pair loop: 0 = auto, 1 = scalar FP32 (two
                             bodies per thread), 2 = packed f32x2 with one pair of bodies
-                            per thread, 4 = packed with two pairs; the packed loops need
-                            uniform masses (per-body masses run the scalar loop) */
+                            per thread, 3 = packed with one body per thread and pairs of
+                            partners, 4 = packed with two pairs of bodies; the packed
+                            loops need uniform masses (per-body masses run the scalar
+                            loop) */
 } gb_force_tiling;
 
 int gb_nbody_rhs_f64(const double* x_dev, double* dxdt_dev, int64_t n_particles,

@@ -501,6 +501,181 @@ __device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict_
 }
 
 // ---------------------------------------------------------------------------
+// Packed form with one body per thread and pairs of partners: each f32x2
+// instruction carries partners j and j + 1 of the same body, so the staged
+// partner records need no duplicated coordinates and a CTA of T threads holds
+// T / L bodies (twice the warps of the two-bodies-per-thread form for the same
+// bodies, which hides more latency on small systems).  Tiles of 2T partners
+// are copied with cp.async into a double-buffered raw area (no registers held
+// across the compute loop); each thread copies two partners and builds one
+// record from them.  A missing second partner (odd tail) is placed at 1e18:
+// its r^-3 underflows to zero, so its term is exactly zero.
+// ---------------------------------------------------------------------------
+struct __align__(16) PartnerPair {
+  ulonglong2 xy;  // (hx_j, hx_j+1), (hy_j, hy_j+1)
+  ulonglong2 zl;  // (hz_j, hz_j+1), (lx_j, lx_j+1)
+  ulonglong2 yz;  // (ly_j, ly_j+1), (lz_j, lz_j+1)
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// Shared memory of force_mixed_cta_jp: T records + 2 x 2T raw bodies.
+template <int T>
+constexpr int jp_smem_bytes() {
+  return (int)sizeof(PartnerPair) * T + 2 * 2 * T * (int)sizeof(PackedBody);
+}
+
+template <int T, int L>
+__device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict__ packed,
+                                                   long long n, long long i0, long long jb,
+                                                   long long je, float eps2, unsigned char* smem,
+                                                   double (*part)[3]) {
+  constexpr int BG = T / L;  // bodies per CTA
+  constexpr int JT = 2 * T;  // partners per tile
+  PartnerPair* rec = reinterpret_cast<PartnerPair*>(smem);
+  PackedBody* raw = reinterpret_cast<PackedBody*>(smem + sizeof(PartnerPair) * T);
+  const int g = threadIdx.x / L;
+  const int l = threadIdx.x % L;
+  const long long i = i0 + g;
+  PackedBody pb;
+  if (i < n) {
+    pb = packed[i];
+  } else {
+    pb.hw = make_float4(0.f, 0.f, 0.f, 0.f);
+    pb.lo = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  const f2_t HX = f2_pack(pb.hw.x, pb.hw.x), HY = f2_pack(pb.hw.y, pb.hw.y),
+             HZ = f2_pack(pb.hw.z, pb.hw.z);
+  const f2_t LX = f2_pack(pb.lo.x, pb.lo.x), LY = f2_pack(pb.lo.y, pb.lo.y),
+             LZ = f2_pack(pb.lo.z, pb.lo.z);
+  const f2_t E2 = f2_pack(eps2, eps2);
+  const int near2 = near_threshold_bits(pb.hw.x, pb.hw.y, pb.hw.z);
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  // this thread copies partners j0 + 2t and j0 + 2t + 1 of every tile
+  auto issue = [&](long long j0, int buf) {
+    PackedBody* dst = raw + buf * JT + 2 * threadIdx.x;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const long long j = j0 + 2 * threadIdx.x + h;
+      if (j < je) {
+        cp_async16(&dst[h].hw, &packed[j].hw);
+        cp_async16(&dst[h].lo, &packed[j].lo);
+      }
+    }
+    cp_async_commit();
+  };
+  if (jb < je) issue(jb, 0);
+  int buf = 0;
+  for (long long j0 = jb; j0 < je; j0 += JT, buf ^= 1) {
+    const int cnt = (int)min((long long)JT, je - j0);
+    const int npair = (cnt + 1) / 2;
+    cp_async_wait_all();  // this thread's own copies of the tile have landed
+    __syncthreads();      // every thread is done with the previous records
+    if (threadIdx.x < npair) {
+      const PackedBody a = raw[buf * JT + 2 * threadIdx.x];
+      PackedBody b;
+      if (2 * threadIdx.x + 1 < cnt) {
+        b = raw[buf * JT + 2 * threadIdx.x + 1];
+      } else {
+        b.hw = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+        b.lo = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      PartnerPair r;
+      r.xy = make_ulonglong2(f2_pack(a.hw.x, b.hw.x), f2_pack(a.hw.y, b.hw.y));
+      r.zl = make_ulonglong2(f2_pack(a.hw.z, b.hw.z), f2_pack(a.lo.x, b.lo.x));
+      r.yz = make_ulonglong2(f2_pack(a.lo.y, b.lo.y), f2_pack(a.lo.z, b.lo.z));
+      rec[threadIdx.x] = r;
+    }
+    __syncthreads();
+    if (j0 + JT < je) issue(j0 + JT, buf ^ 1);  // next tile lands while this one computes
+    f2_t TX = 0ULL, TY = 0ULL, TZ = 0ULL;
+    const int kn = (npair - l + L - 1) / L;
+    for (int k0 = 0; k0 < kn; k0 += 32) {
+      const int kc = min(32, kn - k0);
+      unsigned mask = 0;
+#pragma unroll 4
+      for (int u = 0; u < kc; ++u) {
+        const int jj = l + (k0 + u) * L;
+        const ulonglong2 xy = rec[jj].xy;
+        const f2_t hz = rec[jj].zl.x;
+        const f2_t dx = f2_sub(xy.x, HX);
+        const f2_t dy = f2_sub(xy.y, HY);
+        const f2_t dz = f2_sub(hz, HZ);
+        const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+        float ra, rb;
+        f2_unpack(r2, ra, rb);
+        const bool close = (__float_as_int(ra) < near2) | (__float_as_int(rb) < near2);
+        mask |= (unsigned)close << u;
+        const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+        const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+        TX = f2_fma(sc, dx, TX);
+        TY = f2_fma(sc, dy, TY);
+        TZ = f2_fma(sc, dz, TZ);
+      }
+      while (mask) {
+        const int u = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int jj = l + (k0 + u) * L;
+        const ulonglong2 xy = rec[jj].xy;
+        const ulonglong2 zl = rec[jj].zl;
+        const ulonglong2 yz = rec[jj].yz;
+        f2_t dx = f2_sub(xy.x, HX);
+        f2_t dy = f2_sub(xy.y, HY);
+        f2_t dz = f2_sub(zl.x, HZ);
+        f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+        float ra, rb;
+        f2_unpack(r2, ra, rb);
+        f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+        const f2_t nsc = f2_mul(f2_mul(ri, f2_mul(ri, ri)), f2_pack(-1.f, -1.f));
+        TX = f2_fma(nsc, dx, TX);  // take the hi-only terms out again
+        TY = f2_fma(nsc, dy, TY);
+        TZ = f2_fma(nsc, dz, TZ);
+        dx = f2_add(dx, f2_sub(zl.y, LX));
+        dy = f2_add(dy, f2_sub(yz.x, LY));
+        dz = f2_add(dz, f2_sub(yz.y, LZ));
+        r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+        f2_unpack(r2, ra, rb);
+        ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+        const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+        TX = f2_fma(sc, dx, TX);
+        TY = f2_fma(sc, dy, TY);
+        TZ = f2_fma(sc, dz, TZ);
+      }
+    }
+    float t0, t1;
+    f2_unpack(TX, t0, t1);
+    kahan_add(sx, cx, t0);
+    kahan_add(sx, cx, t1);
+    f2_unpack(TY, t0, t1);
+    kahan_add(sy, cy, t0);
+    kahan_add(sy, cy, t1);
+    f2_unpack(TZ, t0, t1);
+    kahan_add(sz, cz, t0);
+    kahan_add(sz, cz, t1);
+  }
+  double ax = dsub((double)sx, (double)cx);
+  double ay = dsub((double)sy, (double)cy);
+  double az = dsub((double)sz, (double)cz);
+  ax = lane_reduce<L>(ax);
+  ay = lane_reduce<L>(ay);
+  az = lane_reduce<L>(az);
+  if (l == 0) {
+    part[g][0] = ax;
+    part[g][1] = ay;
+    part[g][2] = az;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Mixed precision on spatially sorted bodies.  Bodies are processed in a
 // Morton order, so consecutive 128-body tiles are compact.  Each j-tile J
 // carries its centroid c_J (hi/lo FP32 parts of c_J - c) and radius R_J, and
@@ -661,7 +836,8 @@ __device__ __forceinline__ PackedBody pack_body(double x, double y, double z, do
 
 // Launch geometry shared by the standalone and fused kernels.
 // Mixed pair loop used when the tiling leaves the choice open (1 scalar,
-// 2 / 4 packed with one / two pairs of bodies per thread).
+// 2 / 4 packed with one / two pairs of bodies per thread, 3 packed with one
+// body per thread and pairs of partners).
 constexpr int kDefaultMixedVariant = 2;
 
 struct ForceGeom {

@@ -89,10 +89,11 @@ def test_acc_write_and_accumulate(gb, orc, torch_cuda):
     np.testing.assert_array_equal(acc.cpu().numpy(), 2 * ref)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 4])
+@pytest.mark.parametrize("variant", [0, 1, 3, 4])
 @pytest.mark.parametrize("n,soft,gen", [(1024, 0.01, "ball"), (4096, 0.005, "plummer"),
                                         (16384, 0.005, "plummer"), (3001, 0.003, "binary"),
-                                        (8192, 0.002, "cold")])
+                                        (8192, 0.002, "cold"), (7, 0.05, "plummer"),
+                                        (257, 0.02, "plummer")])
 def test_rhs_mixed_within_1e6_of_fp64(gb, torch_cuda, n, soft, gen, variant):
     """Hi-only pair differences with hi/lo for close pairs, every pair loop:
     accelerations within 1e-6 of FP64 (normwise and for the median body)."""
