@@ -838,7 +838,7 @@ __device__ __forceinline__ PackedBody pack_body(double x, double y, double z, do
 // Mixed pair loop used when the tiling leaves the choice open (1 scalar,
 // 2 / 4 packed with one / two pairs of bodies per thread, 3 packed with one
 // body per thread and pairs of partners).
-constexpr int kDefaultMixedVariant = 2;
+constexpr int kDefaultMixedVariant = 3;
 
 struct ForceGeom {
   int T;      // threads per CTA

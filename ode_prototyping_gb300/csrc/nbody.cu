@@ -280,15 +280,17 @@ ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling,
     if (!uniform_masses) v = 1;
     g.variant = v;
     g.BPT = v == 4 ? 4 : (v == 3 ? 1 : 2);
-    // ~16 warps per SM, each lane pair-loop at least ~256 partners long;
-    // lanes only when the cluster split leaves the grid well short of that
-    // (measured: N = 16384 runs fastest at 8 ranks x 1 lane, N = 65536 at 4 x 1).
-    long long want = (long long)sms * 16 * 32 * g.BPT;
+    // ~32 warps' worth of two-body threads per SM, each lane pair-loop at
+    // least ~256 partners long; lanes only when the cluster split leaves the
+    // grid well short of that (measured with the partner-pair loop: N = 4096
+    // runs fastest at 8 ranks x 2 lanes, N = 16384 at 8 x 1, N = 65536 at 4 x 1).
+    long long want = (long long)sms * 16 * 32 * 2;
     long long lp = (want + n - 1) / n;
     int P = 1;
     while (P < 8 && P < lp && n / (2 * P) >= 256) P *= 2;
     int L = 1;
-    while (L < 4 && 2LL * P * L < lp && n / (2 * P * L) >= 128) L *= 2;
+    const int lmax = g.BPT == 1 ? 2 : 4;
+    while (L < lmax && 2LL * P * L < lp && n / (2 * P * L) >= 128) L *= 2;
     g.P = P;
     g.L = L;
   }
