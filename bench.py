@@ -2,8 +2,9 @@
 
 Workload (one GPU): one N = 16384 Plummer sphere (scale radius 1, velocities
 from the distribution function, seed 101), softening 0.005, the 13-stage
-Fehlberg 7(8) pair, atol = rtol = 1e-8, t in [0, 2], FP32 hi/lo pair forces
-with Kahan-compensated accumulation, FP64 state / stage combination / norm.
+Fehlberg 7(8) pair, atol = rtol = 1e-8, t in [0, 2], FP32 pair forces on
+hi/lo positions (hi/lo differences for close pairs) with Kahan-compensated
+accumulation, FP64 state / stage combination / norm.
 A step is one whole integration t = 0 -> 2 from the seeded state (about 150
 adaptive attempts): the initial-step estimate on the device, then attempts of
 13 fused stage kernels (force + next-stage combination) and one controller
@@ -55,6 +56,9 @@ FLOPS_PER_INTERACTION = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) conven
 # convention counts 10 FMA-equivalents, so the FP32 pipe caps the fraction
 # near 10/11.5.
 HILO_FP32_OPS = 11.5
+# DRAM bytes (read + write) of one headline stage launch from an ncu capture
+# of the same kernel and geometry (python bench.py --workload stage).
+STAGE_DRAM_BYTES_16384 = 2551296
 FP64_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (non-tensor), one FMA = 2 FLOP
 
 
@@ -250,10 +254,11 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--controller", default="reference", choices=["reference", "pi", "learned"])
     ap.add_argument("--mlp", default=None, help="trained proposer weights (learned controller)")
+    ap.add_argument("--n-bodies", type=int, default=16384, help="stage: bodies")
     ap.add_argument("--learned-config", default="plummer4096_rkf78",
                     help="c4: proposer training/evaluation configuration")
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c2_f64", "c1", "c3", "c4", "c5a", "c5b", "rk_hbm"],
+                    choices=["c2", "c2_f64", "c1", "c3", "c4", "c5a", "c5b", "rk_hbm", "stage"],
                     help="c2 (default, the headline), or another configuration")
     args = ap.parse_args()
     world, rank, local = dist_setup()
@@ -369,7 +374,11 @@ def main():
         "clocks": clocks,
         "gpu_launches": args.steps * launches_per_job,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                     "traffic": STAGE_DRAM_BYTES_16384 if n == 16384 else None,
+                     "traffic_note": "DRAM bytes per launch from one ncu capture of this "
+                                     "kernel (compute-bound: positions + stage rows mostly "
+                                     "served from L2)",
                      "kernel": "fused_stage_kernel (mixed, one stage)",
                      "kernel_ms": k_ms, "geometry": geo,
                      "peak_note": f"nominal FP32 pipe: {n_sm} SMs x {FP32_LANES_PER_SM} lanes x 2"
@@ -527,6 +536,26 @@ def run_other_workload(args):
                             "n_min": int(sizes.min()), "n_max": int(sizes.max()),
                             "bodies": int(sizes.sum()), "tableau": tab, "atol": tol,
                             "rtol": tol, "t": [0, tf], "step": "whole batch integration"})
+    elif args.workload == "stage":
+        # Four stage launches of the headline integrator on an N-body Plummer
+        # sphere (a small case for profiling the fused stage kernel).
+        n = args.n_bodies
+        x0 = gb.to_device(gb.ic_plummer(n, WORKLOAD["seed"], 1.0))
+        it = gb.Integrator(WORKLOAD["tableau"], gb.NBodyODE(n, WORKLOAD["softening"], 1.0 / n),
+                           gb.Gb300Executor(precision="mixed", attempts_per_sync=1),
+                           stream=stream)
+        it.start(x0, WORKLOAD["t0"], WORKLOAD["tf"], WORKLOAD["atol"], WORKLOAD["rtol"])
+        ms, _ = _timed(torch, stream, lambda: it.launch_stage(1), 1, flush)
+        with torch.cuda.stream(stream):
+            for r in range(3):
+                it.launch_stage(2 + r)
+        stream.synchronize()
+        line.update(metric="fused stage kernel, one launch", unit="ms", value=ms,
+                    higher_is_better=False, dtype="f32+f64", steps=1, ms_per_step=ms,
+                    geometry=it.geometry(),
+                    config={"workload": f"plummer{n}_rkf78_mixed_stage", "n_particles": n,
+                            "step": "one fused stage launch (four launched)"})
+        it.close()
     elif args.workload == "c4":
         # Learned step-size proposer: trained on seed set A (weights shipped in
         # ode_prototyping_gb300/weights/, retrained here if absent), evaluated

@@ -384,7 +384,10 @@ int gb_integrate_nbody(const gb_tableau* tab, const gb_nbody_system* sys,
 typedef struct {
   int32_t threads_per_cta;   /* 64, 128, 256 (0 = 128) */
   int32_t lanes;             /* lanes per body: 1, 2, 4 (0 = 2) */
-  int32_t bodies_per_thread; /* 1 or 2 (mixed precision; 0 = 1) */
+  int32_t bodies_per_thread; /* mixed precision: 1 = packed f32x2 loop over pairs of
+                                partners (threads_per_cta <= 128; scalar FP32 loop at
+                                256), 2 = scalar FP32 loop with two bodies per thread
+                                (0 = 1) */
   int32_t grid_ctas;         /* persistent grid (0 = 8 CTAs per SM) */
 } gb_batch_tiling;
 

@@ -79,7 +79,10 @@ __global__ void __launch_bounds__(T)
     batch_stage_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ BatchParams P, int s) {
   constexpr int BI = (T / L) * BPT;
-  constexpr int SMEM_BODY_BYTES = PREC == GB_PREC_F64 ? 32 * T : (int)sizeof(PackedBody) * T;
+  // one body per thread (T <= 128): the packed loop over pairs of partners
+  constexpr bool PK = PREC == GB_PREC_MIXED && BPT == 1 && T <= 128;
+  constexpr int SMEM_BODY_BYTES =
+      PREC == GB_PREC_F64 ? 32 * T : (PK ? jp_smem_bytes<T>() : (int)sizeof(PackedBody) * T);
   __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
   __shared__ double part[BI][3];
   __shared__ double red[T];
@@ -106,8 +109,11 @@ __global__ void __launch_bounds__(T)
       } else {
         const PackedBody* src = (s == 0) ? P.PX + (long long)px * P.total_bodies + sy.body_off
                                          : P.PY + (long long)(s & 1) * P.total_bodies + sy.body_off;
-        force_mixed_cta<T, L, BPT, true>(src, n, i0, 0, n, sy.eps2f,
-                                         reinterpret_cast<PackedBody*>(sh_raw), part);
+        if constexpr (PK)
+          force_mixed_cta_jp<T, L>(src, n, i0, 0, n, sy.eps2f, sh_raw, part);
+        else
+          force_mixed_cta<T, L, BPT, true>(src, n, i0, 0, n, sy.eps2f,
+                                           reinterpret_cast<PackedBody*>(sh_raw), part);
       }
     }
     __syncthreads();
@@ -211,7 +217,10 @@ __global__ void __launch_bounds__(T)
     batch_rhs_kernel(const __grid_constant__ BatchParams P, const double* __restrict__ x,
                      const PackedBody* __restrict__ packed, double* __restrict__ out) {
   constexpr int BI = (T / L) * BPT;
-  constexpr int SMEM_BODY_BYTES = PREC == GB_PREC_F64 ? 32 * T : (int)sizeof(PackedBody) * T;
+  // one body per thread (T <= 128): the packed loop over pairs of partners
+  constexpr bool PK = PREC == GB_PREC_MIXED && BPT == 1 && T <= 128;
+  constexpr int SMEM_BODY_BYTES =
+      PREC == GB_PREC_F64 ? 32 * T : (PK ? jp_smem_bytes<T>() : (int)sizeof(PackedBody) * T);
   __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
   __shared__ double part[BI][3];
   for (long long u = blockIdx.x; u < P.n_units; u += gridDim.x) {
@@ -224,8 +233,11 @@ __global__ void __launch_bounds__(T)
       double* sh_pos = reinterpret_cast<double*>(sh_raw);
       force_f64_cta<T, L>(xs, n, i0, 0, n, sy.eps2, nullptr, sh_pos, sh_pos + 3 * T, part);
     } else {
-      force_mixed_cta<T, L, BPT, true>(packed + sy.body_off, n, i0, 0, n, sy.eps2f,
-                                       reinterpret_cast<PackedBody*>(sh_raw), part);
+      if constexpr (PK)
+        force_mixed_cta_jp<T, L>(packed + sy.body_off, n, i0, 0, n, sy.eps2f, sh_raw, part);
+      else
+        force_mixed_cta<T, L, BPT, true>(packed + sy.body_off, n, i0, 0, n, sy.eps2f,
+                                         reinterpret_cast<PackedBody*>(sh_raw), part);
     }
     __syncthreads();
     const long long nb = min((long long)BI, n - i0);
