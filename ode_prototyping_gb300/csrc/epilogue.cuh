@@ -107,8 +107,8 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
 #pragma unroll
     for (int e = 0; e < 6; ++e) v[e] = 0.0;
     for (int l = 0; l <= s; ++l) {
+      if (!((tab.anz[s] >> l) & 1u)) continue;
       const double a = tab.a[s][l];
-      if (a == 0.0) continue;
       double kl[6];
       if (l == s) {
 #pragma unroll
@@ -139,8 +139,9 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
 #pragma unroll
     for (int e = 0; e < 6; ++e) xv[e] = ev[e] = 0.0;
     for (int l = 0; l < S; ++l) {
+      const unsigned bl = (tab.bnz >> l) & 1u, dl = (tab.dbnz >> l) & 1u;
+      if (!(bl | dl)) continue;
       const double bb = tab.b[l], db = tab.db[l];
-      if (bb == 0.0 && db == 0.0) continue;
       double kl[6];
       if (l == s) {
 #pragma unroll
@@ -152,8 +153,8 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
       }
 #pragma unroll
       for (int e = 0; e < 6; ++e) {
-        if (bb != 0.0) xv[e] = dadd(xv[e], dmul(bb, kl[e]));
-        if (db != 0.0) ev[e] = dadd(ev[e], dmul(db, kl[e]));
+        if (bl) xv[e] = dadd(xv[e], dmul(bb, kl[e]));
+        if (dl) ev[e] = dadd(ev[e], dmul(db, kl[e]));
       }
     }
 #pragma unroll

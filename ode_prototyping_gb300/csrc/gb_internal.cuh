@@ -46,6 +46,11 @@ struct DevTableau {
   double a[GB_MAX_STAGES][GB_MAX_STAGES];
   double b[GB_MAX_STAGES];
   double db[GB_MAX_STAGES];
+  // non-zero patterns (bit j set when the coefficient of k_j is not zero),
+  // so device code tests integer bits instead of comparing doubles (an FP64
+  // compare occupies the FP64 pipe like a multiply)
+  unsigned anz[GB_MAX_STAGES];  // row s-1 of a: coefficients of stage s
+  unsigned bnz, dbnz;
 };
 DevTableau make_dev_tableau(const gb_tableau& t);
 

@@ -50,6 +50,13 @@ DevTableau make_dev_tableau(const gb_tableau& t) {
   std::memcpy(d.a, t.a, sizeof d.a);
   std::memcpy(d.b, t.b, sizeof d.b);
   for (int j = 0; j < GB_MAX_STAGES; ++j) d.db[j] = t.b[j] - t.bt[j];
+  for (int r = 0; r < GB_MAX_STAGES; ++r)
+    for (int j = 0; j < GB_MAX_STAGES; ++j)
+      if (t.a[r][j] != 0.0) d.anz[r] |= 1u << j;
+  for (int j = 0; j < GB_MAX_STAGES; ++j) {
+    if (d.b[j] != 0.0) d.bnz |= 1u << j;
+    if (d.db[j] != 0.0) d.dbnz |= 1u << j;
+  }
   const int S = t.n_stages;
   int fsal = S >= 2 && t.b[S - 1] == 0.0;
   for (int j = 0; fsal && j < S - 1; ++j)
@@ -74,6 +81,7 @@ unsigned blocks_for(long long n) {
 struct Coef {
   double c[GB_MAX_STAGES];
   double d[GB_MAX_STAGES];
+  unsigned cnz, dnz;  // bit j: c[j] (d[j]) is not zero; tested as integers on the device
 };
 
 // V consecutive doubles per thread and iteration (V = 2: 16-byte loads).
@@ -113,7 +121,7 @@ __global__ void __launch_bounds__(kBlock) stage_kernel(const __grid_constant__ C
     Vec<V> k[S], x;
 #pragma unroll
     for (int j = 0; j < S; ++j)
-      if (cf.c[j] != 0.0) k[j].load(ks + (long long)j * n, e);
+      if ((cf.cnz >> j) & 1u) k[j].load(ks + (long long)j * n, e);
     x.load(x0, e);
     Vec<V> out;
 #pragma unroll
@@ -121,7 +129,7 @@ __global__ void __launch_bounds__(kBlock) stage_kernel(const __grid_constant__ C
       double v = 0.0;
 #pragma unroll
       for (int j = 0; j < S; ++j)
-        if (cf.c[j] != 0.0) v = dadd(v, dmul(cf.c[j], k[j].v[u]));
+        if ((cf.cnz >> j) & 1u) v = dadd(v, dmul(cf.c[j], k[j].v[u]));
       out.v[u] = dadd(x.v[u], dmul(v, dt));
     }
     out.store(temp, e);
@@ -142,7 +150,7 @@ __global__ void __launch_bounds__(kBlock) update_kernel(const __grid_constant__ 
     Vec<V> k[S], x0v;
 #pragma unroll
     for (int j = 0; j < S; ++j)
-      if (cf.c[j] != 0.0 || cf.d[j] != 0.0) k[j].load(ks + (long long)j * n, e);
+      if (((cf.cnz | cf.dnz) >> j) & 1u) k[j].load(ks + (long long)j * n, e);
     x0v.load(x0, e);
     Vec<V> xo, eo;
 #pragma unroll
@@ -150,8 +158,8 @@ __global__ void __launch_bounds__(kBlock) update_kernel(const __grid_constant__ 
       double xv = 0.0, ev = 0.0;
 #pragma unroll
       for (int j = 0; j < S; ++j) {
-        if (cf.c[j] != 0.0) xv = dadd(xv, dmul(cf.c[j], k[j].v[u]));
-        if (cf.d[j] != 0.0) ev = dadd(ev, dmul(cf.d[j], k[j].v[u]));
+        if ((cf.cnz >> j) & 1u) xv = dadd(xv, dmul(cf.c[j], k[j].v[u]));
+        if ((cf.dnz >> j) & 1u) ev = dadd(ev, dmul(cf.d[j], k[j].v[u]));
       }
       xo.v[u] = dadd(x0v.v[u], dmul(xv, dt));
       eo.v[u] = dmul(ev, dt);
@@ -493,7 +501,10 @@ extern "C" int gb_rk_stage_f64(const gb_tableau* tab, int32_t stage, double dt, 
     return GB_ERR_INVALID_ARGUMENT;
   Coef cf;
   std::memset(&cf, 0, sizeof cf);
-  for (int j = 0; j < stage; ++j) cf.c[j] = tab->a[stage - 1][j];
+  for (int j = 0; j < stage; ++j) {
+    cf.c[j] = tab->a[stage - 1][j];
+    if (cf.c[j] != 0.0) cf.cnz |= 1u << j;
+  }
   cudaStream_t st = as_cuda(stream);
   if (n % 2 == 0 && aligned16(x0) && aligned16(ks) && aligned16(temp))
     launch_stage_v<2>(stage, cf, dt, x0, ks, temp, n, st);
@@ -513,6 +524,8 @@ extern "C" int gb_rk_update_state_and_error_f64(const gb_tableau* tab, double dt
   for (int j = 0; j < tab->n_stages; ++j) {
     cf.c[j] = tab->b[j];
     cf.d[j] = tab->b[j] - tab->bt[j];
+    if (cf.c[j] != 0.0) cf.cnz |= 1u << j;
+    if (cf.d[j] != 0.0) cf.dnz |= 1u << j;
   }
   cudaStream_t st = as_cuda(stream);
   if (n % 2 == 0 && aligned16(x0) && aligned16(ks) && aligned16(x) && aligned16(err))
