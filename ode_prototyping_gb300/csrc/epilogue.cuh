@@ -106,6 +106,7 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
     double yn[6], v[6];
 #pragma unroll
     for (int e = 0; e < 6; ++e) v[e] = 0.0;
+#pragma unroll 1
     for (int l = 0; l <= s; ++l) {
       if (!((tab.anz[s] >> l) & 1u)) continue;
       const double a = tab.a[s][l];
@@ -138,6 +139,7 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
     double xn[6], xv[6], ev[6];
 #pragma unroll
     for (int e = 0; e < 6; ++e) xv[e] = ev[e] = 0.0;
+#pragma unroll 1
     for (int l = 0; l < S; ++l) {
       const unsigned bl = (tab.bnz >> l) & 1u, dl = (tab.dbnz >> l) & 1u;
       if (!(bl | dl)) continue;

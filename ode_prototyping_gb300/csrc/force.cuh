@@ -85,6 +85,36 @@ __device__ __forceinline__ void cluster_combine(double (*part)[3], int rank, int
   cl.sync();
 }
 
+// Cluster-wide combine that leaves every rank the totals of its own rows:
+// rank r owns rows [r R, (r + 1) R), R = ceil(BI / size), and adds the ranks'
+// partial sums in the order of cluster_combine (rank 0's value, then ranks
+// 1, ..., size - 1), so the totals are bit-identical to it.  No rank reads
+// another's rows inside that rank's own range, so each rank overwrites its
+// rows in place.  All threads of all CTAs of the cluster must call it.
+template <int BI>
+__device__ __forceinline__ void cluster_combine_rows(double (*part)[3], int rank, int size) {
+  cg::cluster_group cl = cg::this_cluster();
+  cl.sync();
+  if (size > 1) {
+    const int R = (BI + size - 1) / size;
+    const int lo = rank * R, hi = min(BI, lo + R);
+    double(*p0)[3] = cl.map_shared_rank(part, 0);
+    for (int b = lo + (int)threadIdx.x; b < hi; b += blockDim.x) {
+      double s0 = p0[b][0], s1 = p0[b][1], s2 = p0[b][2];
+      for (int r = 1; r < size; ++r) {
+        double(*rp)[3] = cl.map_shared_rank(part, r);
+        s0 = dadd(s0, rp[b][0]);
+        s1 = dadd(s1, rp[b][1]);
+        s2 = dadd(s2, rp[b][2]);
+      }
+      part[b][0] = s0;
+      part[b][1] = s1;
+      part[b][2] = s2;
+    }
+  }
+  cl.sync();
+}
+
 // ---------------------------------------------------------------------------
 // FP64: partial sums of one CTA over its partner chunk.  sh_pos holds 3*T
 // doubles, sh_m T doubles (per-body masses only).  Results land in part[b].
@@ -613,8 +643,11 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
         const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
         float ra, rb;
         f2_unpack(r2, ra, rb);
-        const bool close = (__float_as_int(ra) < near2) | (__float_as_int(rb) < near2);
-        mask |= (unsigned)close << u;
+        // both partners share the body's threshold: one comparison of the
+        // smaller bit pattern, shifted in (bit b of the chunk's mask is
+        // iteration kc - 1 - b)
+        mask = (mask << 1) |
+               (unsigned)(min(__float_as_int(ra), __float_as_int(rb)) < near2);
         const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
         const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
         TX = f2_fma(sc, dx, TX);
@@ -622,7 +655,7 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
         TZ = f2_fma(sc, dz, TZ);
       }
       while (mask) {
-        const int u = __ffs(mask) - 1;
+        const int u = kc - __ffs(mask);
         mask &= mask - 1;
         const int jj = l + (k0 + u) * L;
         const ulonglong2 xy = rec[jj].xy;

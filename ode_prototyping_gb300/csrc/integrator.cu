@@ -36,7 +36,7 @@ size_t norm_workspace_bytes(long long n);
 namespace {
 
 template <int PREC, int T, int L, int BPT, bool PACKED = false>
-__global__ void __launch_bounds__(T, PACKED && BPT <= 2 ? 7 * 128 / T : (PACKED ? 4 * 128 / T : 1))
+__global__ void __launch_bounds__(T, PACKED && BPT <= 2 ? 7 * 128 / T : (PACKED ? 4 * 128 / T : 5 * 128 / T))
     fused_stage_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ FusedParams P, int s) {
   constexpr int BI = (T / L) * BPT;
@@ -84,11 +84,12 @@ __global__ void __launch_bounds__(T, PACKED && BPT <= 2 ? 7 * 128 / T : (PACKED 
                                          reinterpret_cast<PackedBody*>(sh_raw), part);
       }
     }
-    cluster_combine<BI>(part, ci.rank, ci.size);
+    cluster_combine_rows<BI>(part, ci.rank, ci.size);
   }
-  if (ci.rank != 0) return;
-
-  const long long nb = min((long long)BI, n - i0);
+  // every cluster rank finishes its own rows of the i-tile
+  const int rows = (BI + ci.size - 1) / ci.size;
+  const int b_lo = ci.rank * rows;
+  const int b_hi = (int)min((long long)min(BI, b_lo + rows), n - i0);
   const bool last = (s == S - 1);
   EpiCtx E;
   E.tab = &tab;
@@ -117,14 +118,16 @@ __global__ void __launch_bounds__(T, PACKED && BPT <= 2 ? 7 * 128 / T : (PACKED 
   E.sq = P.sq;
   double sq_acc = 0.0;
   double amax = 0.0;
-  for (int b = threadIdx.x; b < nb; b += T) body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
+#pragma unroll 1
+  for (int b = b_lo + (int)threadIdx.x; b < b_hi; b += T)
+    body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
   if (last) {
     const double m = block_max(amax, red);
-    if (threadIdx.x == 0) P.aux[ci.itile] = m;
+    if (threadIdx.x == 0) P.aux[ci.itile * ci.size + ci.rank] = m;
   }
   if (!last) return;
   const double tile_sum = block_sum(sq_acc, red);
-  if (threadIdx.x == 0) P.partials[ci.itile] = tile_sum;
+  if (threadIdx.x == 0) P.partials[ci.itile * ci.size + ci.rank] = tile_sum;
 }
 
 // The mixed-precision stage on Morton-sorted tiles: i-tile = 128 consecutive
@@ -209,11 +212,11 @@ __global__ void __launch_bounds__(T, 768 / T)
   pack_sorted_tile(np, valid, (int)nb, w, P.cref, near_out, far_out, meta_out, red);
   if (last) {
     const double m = block_max(amax, red);
-    if (threadIdx.x == 0) P.aux[ci.itile] = m;
+    if (threadIdx.x == 0) P.aux[ci.itile * ci.size] = m;
   }
   if (!last) return;
   const double tile_sum = block_sum(sq_acc, red);
-  if (threadIdx.x == 0) P.partials[ci.itile] = tile_sum;
+  if (threadIdx.x == 0) P.partials[ci.itile * ci.size] = tile_sum;
 }
 
 // Dense output of DOPRI5 (the continuous extension of Dormand & Prince as
@@ -287,14 +290,14 @@ __global__ void __launch_bounds__(256)
     __syncthreads();
   } else {
     double v = 0.0;
-    for (long long k = threadIdx.x; k < P.n_itiles; k += T) v = dadd(v, P.partials[k]);
+    for (long long k = threadIdx.x; k < P.n_parts; k += T) v = dadd(v, P.partials[k]);
     total = block_sum(v, red);
   }
   const int k0_valid = C->k0_valid;
   double amax_all = 0.0;
   {
     double v = 0.0;
-    for (long long k = threadIdx.x; k < P.n_itiles; k += T) v = fmax(v, P.aux[k]);
+    for (long long k = threadIdx.x; k < P.n_parts; k += T) v = fmax(v, P.aux[k]);
     amax_all = block_max(v, red);
   }
   const double err = sqrt(total / (double)n_var);
@@ -806,8 +809,16 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   GB_ALLOC(it->ks, (size_t)it->S * nv * sizeof(double));
   GB_ALLOC(it->Y, (size_t)2 * nv * sizeof(double));
   GB_ALLOC(it->cref, 4 * sizeof(double));
-  GB_ALLOC(it->partials, (size_t)it->geom.n_itiles * sizeof(double));
-  GB_ALLOC(it->aux, (size_t)it->geom.n_itiles * sizeof(double));
+  // one partial per (i-tile, cluster rank); entries a kernel does not write stay 0
+  const size_t n_parts = (size_t)it->geom.n_itiles * it->geom.P;
+  GB_ALLOC(it->partials, n_parts * sizeof(double));
+  GB_ALLOC(it->aux, n_parts * sizeof(double));
+  e = cudaMemset(it->partials, 0, n_parts * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(it->aux, 0, n_parts * sizeof(double));
+  if (e != cudaSuccess) {
+    note_cuda_error(e);
+    return fail(GB_ERR_CUDA);
+  }
   GB_ALLOC(it->dscal, 8 * sizeof(double));
   GB_ALLOC(it->norm_work, norm_workspace_bytes(nv));
   if (opts.exact) GB_ALLOC(it->sq, (size_t)nv * sizeof(double));
@@ -893,6 +904,7 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   P.n = n;
   P.n_var = nv;
   P.n_itiles = it->geom.n_itiles;
+  P.n_parts = it->geom.n_itiles * it->geom.P;
   P.exact = opts.exact;
   P.S = it->S;
   P.perm = it->perm;

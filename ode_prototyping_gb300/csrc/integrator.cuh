@@ -71,13 +71,13 @@ struct FusedParams {
   float eps2f;
   int R;
   const double* cref;  // reference point for hi/lo packing
-  double* partials;    // n_itiles
+  double* partials;    // n_parts: per (i-tile, cluster rank) scaled-square sums
   double* sq;          // n_var (exact mode)
-  double* aux;         // n_itiles (max |a| partials)
+  double* aux;         // n_parts (max |a| partials)
   StepLog* log;        // log_capacity records or null
   long long log_capacity;
   const void* mlp;     // device MLP weights (learned controller) or null
-  long long n, n_var, n_itiles;
+  long long n, n_var, n_itiles, n_parts;
   int exact;
   int S;
   // spatially sorted mixed path
