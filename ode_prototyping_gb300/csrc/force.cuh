@@ -558,10 +558,10 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
 
-// Shared memory of force_mixed_cta_jp: T records + 2 x 2T raw bodies.
+// Shared memory of force_mixed_cta_jp: 2 x T records + 2T raw bodies.
 template <int T>
 constexpr int jp_smem_bytes() {
-  return (int)sizeof(PartnerPair) * T + 2 * 2 * T * (int)sizeof(PackedBody);
+  return 2 * (int)sizeof(PartnerPair) * T + 2 * T * (int)sizeof(PackedBody);
 }
 
 template <int T, int L>
@@ -571,8 +571,8 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
                                                    double (*part)[3]) {
   constexpr int BG = T / L;  // bodies per CTA
   constexpr int JT = 2 * T;  // partners per tile
-  PartnerPair* rec = reinterpret_cast<PartnerPair*>(smem);
-  PackedBody* raw = reinterpret_cast<PackedBody*>(smem + sizeof(PartnerPair) * T);
+  PartnerPair* recs = reinterpret_cast<PartnerPair*>(smem);  // two buffers of T records
+  PackedBody* raw = reinterpret_cast<PackedBody*>(smem + 2 * sizeof(PartnerPair) * T);
   const int g = threadIdx.x / L;
   const int l = threadIdx.x % L;
   const long long i = i0 + g;
@@ -590,9 +590,14 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
   const f2_t E2 = f2_pack(eps2, eps2);
   const int near2 = near_threshold_bits(pb.hw.x, pb.hw.y, pb.hw.z);
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-  // this thread copies partners j0 + 2t and j0 + 2t + 1 of every tile
-  auto issue = [&](long long j0, int buf) {
-    PackedBody* dst = raw + buf * JT + 2 * threadIdx.x;
+  // Thread t copies partners j0 + 2t and j0 + 2t + 1 of every tile into its
+  // own two raw slots and later builds record t from them, so the single raw
+  // area needs no barrier: a thread re-issues its slots only after reading
+  // them (in issue order).  Records are double-buffered: tile k + 1's are
+  // built at the end of tile k into the buffer tile k - 1 used, and one
+  // barrier per tile both publishes them and retires tile k's.
+  auto issue = [&](long long j0) {
+    PackedBody* dst = raw + 2 * threadIdx.x;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const long long j = j0 + 2 * threadIdx.x + h;
@@ -603,18 +608,13 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     }
     cp_async_commit();
   };
-  if (jb < je) issue(jb, 0);
-  int buf = 0;
-  for (long long j0 = jb; j0 < je; j0 += JT, buf ^= 1) {
+  auto build = [&](long long j0, PartnerPair* out) {
     const int cnt = (int)min((long long)JT, je - j0);
-    const int npair = (cnt + 1) / 2;
-    cp_async_wait_all();  // this thread's own copies of the tile have landed
-    __syncthreads();      // every thread is done with the previous records
-    if (threadIdx.x < npair) {
-      const PackedBody a = raw[buf * JT + 2 * threadIdx.x];
+    if ((int)threadIdx.x < (cnt + 1) / 2) {
+      const PackedBody a = raw[2 * threadIdx.x];
       PackedBody b;
-      if (2 * threadIdx.x + 1 < cnt) {
-        b = raw[buf * JT + 2 * threadIdx.x + 1];
+      if (2 * (int)threadIdx.x + 1 < cnt) {
+        b = raw[2 * threadIdx.x + 1];
       } else {
         b.hw = make_float4(1e18f, 1e18f, 1e18f, 0.f);
         b.lo = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -623,10 +623,21 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
       r.xy = make_ulonglong2(f2_pack(a.hw.x, b.hw.x), f2_pack(a.hw.y, b.hw.y));
       r.zl = make_ulonglong2(f2_pack(a.hw.z, b.hw.z), f2_pack(a.lo.x, b.lo.x));
       r.yz = make_ulonglong2(f2_pack(a.lo.y, b.lo.y), f2_pack(a.lo.z, b.lo.z));
-      rec[threadIdx.x] = r;
+      out[threadIdx.x] = r;
     }
-    __syncthreads();
-    if (j0 + JT < je) issue(j0 + JT, buf ^ 1);  // next tile lands while this one computes
+  };
+  if (jb < je) {
+    issue(jb);
+    cp_async_wait_all();
+    build(jb, recs);
+    if (jb + JT < je) issue(jb + JT);
+  }
+  __syncthreads();
+  int buf = 0;
+  for (long long j0 = jb; j0 < je; j0 += JT, buf ^= 1) {
+    const int cnt = (int)min((long long)JT, je - j0);
+    const int npair = (cnt + 1) / 2;
+    const PartnerPair* rec = recs + buf * T;
     f2_t TX = 0ULL, TY = 0ULL, TZ = 0ULL;
     const int kn = (npair - l + L - 1) / L;
     for (int k0 = 0; k0 < kn; k0 += 32) {
@@ -694,6 +705,12 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     f2_unpack(TZ, t0, t1);
     kahan_add(sz, cz, t0);
     kahan_add(sz, cz, t1);
+    if (j0 + JT < je) {
+      cp_async_wait_all();                 // this thread's copies of tile k + 1
+      build(j0 + JT, recs + (buf ^ 1) * T);
+      if (j0 + 2 * JT < je) issue(j0 + 2 * JT);
+    }
+    __syncthreads();
   }
   double ax = dsub((double)sx, (double)cx);
   double ay = dsub((double)sy, (double)cy);
