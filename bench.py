@@ -130,6 +130,39 @@ def load_mlp(args):
     return gb.GbMlp.from_buffer_copy(open(path, "rb").read())
 
 
+def drift(e0: dict, e1: dict) -> dict:
+    """Conservation diagnostics between two states (FP64 device kernel):
+    relative energy error, and the change of total momentum and angular
+    momentum (absolute; both start near zero in the centre-of-mass frame)."""
+    return {"energy_rel_err": abs(e1["e"] - e0["e"]) / abs(e0["e"]),
+            "momentum_drift": float(np.linalg.norm(e1["p"] - e0["p"])),
+            "angular_momentum_drift": float(np.linalg.norm(e1["l"] - e0["l"]))}
+
+
+def c1_cpu_baseline(x0: np.ndarray, n: int, eps: float, tol: float) -> dict:
+    """The reference's thread-pool loop (restated in oracle/) over the whole
+    C1 integration t = 0 -> 1 on all host threads, host clock."""
+    import oracle
+    threads = os.cpu_count() or 1
+    ode, _ = oracle.nbody_ode(n, eps, 1.0 / n)
+    sess = oracle.Session("DOPRI5", ode, x0, 0.0, 1.0, tol, tol, threads)
+    t0 = time.perf_counter()
+    accepted = attempts = 0
+    while True:
+        done, a = sess.attempt()
+        if done:
+            break
+        attempts += 1
+        accepted += int(a)
+    wall = time.perf_counter() - t0
+    sess.close()
+    return {"value": accepted / wall, "unit": "accepted steps/s", "cores": threads,
+            "kind": "port", "seconds": wall, "accepted": accepted, "attempts": attempts,
+            "sample": f"the whole C1 integration (N={n}, DOPRI5, tol {tol:g}, t in [0, 1]) by "
+                      f"the reference thread-pool loop restated in oracle/gbode_oracle.c on "
+                      f"{threads} host threads"}
+
+
 def aggregate_over_ranks(accepted: float, rhs: float, ms: float, device: str = "cuda"):
     """Whole-job totals over replicas (one independent system per GPU):
     accepted steps and RHS evaluations summed, device time = max over ranks."""
@@ -325,7 +358,8 @@ def main():
     ms = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1))
     xs, t_now = it.state()
     e1 = gb.energy(xs, n, eps, 1.0 / n)
-    energy_err = abs(e1["e"] - e0["e"]) / abs(e0["e"])
+    cons = drift(e0, e1)
+    energy_err = cons["energy_rel_err"]
     per_job = {"accepted": accepted // max(args.steps, 1), "attempts": attempts // max(args.steps, 1),
                "rhs_evals": rhs // max(args.steps, 1)}
     # launches per job: start-up kernels + graph replays of A attempts x (S + 1)
@@ -371,6 +405,8 @@ def main():
         "pair_interactions_per_s": pair_rate,
         "per_step": per_job, "rejected_fraction": 1 - accepted / max(attempts, 1),
         "t_reached": t_now, "energy_rel_err": energy_err,
+        "momentum_drift": cons["momentum_drift"],
+        "angular_momentum_drift": cons["angular_momentum_drift"],
         "clocks": clocks,
         "gpu_launches": args.steps * launches_per_job,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
@@ -463,7 +499,7 @@ def run_other_workload(args):
                     pair_interactions_per_s=st[0]["n_rhs"] * n * (n - 1) / (ms / 1e3),
                     per_step={"accepted": st[0]["n_accepted"], "attempts": st[0]["n_attempts"],
                               "rhs": st[0]["n_rhs"]},
-                    energy_rel_err=abs(e1["e"] - e0["e"]) / abs(e0["e"]),
+                    **drift(e0, e1),
                     config={**W, "precision": "f64", "step": "whole integration"})
         it.close()
     elif args.workload == "c1":
@@ -487,7 +523,8 @@ def run_other_workload(args):
                     ms_per_step=ms / args.steps, pair_interactions_per_s=rhs * n * (n - 1) / (ms / 1e3),
                     per_step={"accepted": st[0]["n_accepted"], "attempts": st[0]["n_attempts"],
                               "rhs": st[0]["n_rhs"]},
-                    energy_rel_err=abs(e1["e"] - e0["e"]) / abs(e0["e"]),
+                    **drift(e0, e1),
+                    cpu_baseline=c1_cpu_baseline(gb.ic_uniform_ball(n, 1, 0.1), n, eps, tol),
                     config={"workload": "ball1024_dopri5_f64", "n_particles": n, "softening": eps,
                             "tableau": "DOPRI5", "atol": tol, "rtol": tol, "t": [0, 1],
                             "step": "whole integration"})
@@ -743,7 +780,7 @@ def fp64_compare(gb, torch, x0, line, k: int = 6) -> dict:
         ms = a.elapsed_time(b)
         res[prec] = {"accepted_steps_per_s": (s1["n_accepted"] - s0["n_accepted"]) / (ms / 1e3),
                      "attempts": k, "t_reached": t,
-                     "energy_rel_err": abs(e1["e"] - e0["e"]) / abs(e0["e"]), "ms": ms}
+                     **drift(e0, e1), "ms": ms}
         res[prec + "_state"] = xs
         it.close()
     diff = (res["mixed_state"] - res["f64_state"]).abs().max().item()
