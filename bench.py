@@ -288,10 +288,12 @@ def main():
     ap.add_argument("--controller", default="reference", choices=["reference", "pi", "learned"])
     ap.add_argument("--mlp", default=None, help="trained proposer weights (learned controller)")
     ap.add_argument("--n-bodies", type=int, default=16384, help="stage: bodies")
+    ap.add_argument("--tol", type=float, default=1e-9, help="c2_tol: atol = rtol")
     ap.add_argument("--learned-config", default="plummer4096_rkf78",
                     help="c4: proposer training/evaluation configuration")
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c2_f64", "c1", "c3", "c4", "c5a", "c5b", "rk_hbm", "stage"],
+                    choices=["c2", "c2_f64", "c2_tol", "c1", "c3", "c4", "c5a", "c5b", "rk_hbm",
+                             "stage"],
                     help="c2 (default, the headline), or another configuration")
     args = ap.parse_args()
     world, rank, local = dist_setup()
@@ -502,6 +504,40 @@ def run_other_workload(args):
                     **drift(e0, e1),
                     config={**W, "precision": "f64", "step": "whole integration"})
         it.close()
+    elif args.workload == "c2_tol":
+        # The headline system integrated t = 0 -> 2 by the mixed path and by the
+        # plain FP64 path at a tighter tolerance (--tol), each once: accepted
+        # steps/s and the conservation diagnostics of both, so the two are
+        # compared at an energy error below 1e-8.
+        W = WORKLOAD
+        n, eps = W["n_particles"], W["softening"]
+        x0 = gb.to_device(gb.ic_plummer(n, W["seed"], 1.0))
+        e0 = gb.energy(x0, n, eps, 1.0 / n)
+        res = {}
+        for prec in ("mixed", "f64"):
+            it = gb.Integrator(W["tableau"], gb.NBodyODE(n, eps, 1.0 / n),
+                               gb.Gb300Executor(precision=prec, attempts_per_sync=16),
+                               stream=stream)
+
+            def job():
+                it.start(x0, W["t0"], W["tf"], args.tol, args.tol)
+                assert it.advance(0) == 0
+                return it.stats()
+            if prec == "mixed":
+                job()  # warm-up
+            ms, st = _timed(torch, stream, job, 1, flush)
+            e1 = gb.energy(it.state()[0], n, eps, 1.0 / n)
+            res[prec] = {"accepted_steps_per_s": st[0]["n_accepted"] / (ms / 1e3),
+                         "accepted": st[0]["n_accepted"], "attempts": st[0]["n_attempts"],
+                         "ms": ms, **drift(e0, e1)}
+            it.close()
+        line.update(value=res["mixed"]["accepted_steps_per_s"], dtype="f32+f64", steps=1,
+                    ms_per_step=res["mixed"]["ms"], warmup=1, paths=res,
+                    speedup_mixed_vs_f64=res["mixed"]["accepted_steps_per_s"]
+                    / res["f64"]["accepted_steps_per_s"],
+                    config={**W, "atol": args.tol, "rtol": args.tol,
+                            "workload": "plummer16384_rkf78_tight_tolerance",
+                            "step": "one whole integration per path"})
     elif args.workload == "c1":
         n, eps, tol = 1024, 0.01, 1e-10
         x0 = gb.to_device(gb.ic_uniform_ball(n, 1, 0.1))
