@@ -42,7 +42,7 @@ def test_rhs_f64_tilings_within_1e12(gb, orc, torch_cuda, P, L, B):
     ref = orc.rhs(ode, x)
     got = gb.nbody_rhs_f64(x, n, soft, 1.0 / n, tile=gb.tiling(P, L, B)).cpu().numpy()
     acc_g, acc_r = got[3 * n:].reshape(-1, 3), ref[3 * n:].reshape(-1, 3)
-    # the benchmark spec bound: accelerations agree to <= 1e-12 relative
+    # FP64 parity bound for any tiling: accelerations agree to <= 1e-12 relative
     rel = np.linalg.norm(acc_g - acc_r, axis=1) / np.linalg.norm(acc_r, axis=1)
     assert rel.max() <= 1e-12, rel.max()
     np.testing.assert_array_equal(got[: 3 * n], ref[: 3 * n])
