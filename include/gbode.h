@@ -107,12 +107,11 @@ typedef struct {
                             (0 = auto; 16 is a non-portable cluster size) */
   int32_t lanes;         /* lanes per body inside a warp: 1,2,4,8 (0 = auto) */
   int32_t bodies_per_cta;/* i-bodies per CTA: 32..256 (0 = auto) */
-  int32_t mixed_variant; /* mixed-precision pair loop: 0 = auto, 1 = scalar FP32 (two
-                            bodies per thread), 2 = packed f32x2 with one pair of bodies
-                            per thread, 3 = packed with one body per thread and pairs of
-                            partners, 4 = packed with two pairs of bodies; the packed
-                            loops need uniform masses (per-body masses run the scalar
-                            loop) */
+  int32_t mixed_variant; /* mixed-precision pair loop: 0 = auto (2), 1 = scalar FP32 (two
+                            bodies per thread, any masses), 2 = packed f32x2 over pairs of
+                            partners with two bodies per thread, 3 = the same with one
+                            body per thread; the packed loops need uniform masses
+                            (per-body masses run the scalar loop) */
 } gb_force_tiling;
 
 int gb_nbody_rhs_f64(const double* x_dev, double* dxdt_dev, int64_t n_particles,
@@ -384,10 +383,9 @@ int gb_integrate_nbody(const gb_tableau* tab, const gb_nbody_system* sys,
 typedef struct {
   int32_t threads_per_cta;   /* 64, 128, 256 (0 = 128) */
   int32_t lanes;             /* lanes per body: 1, 2, 4 (0 = 2) */
-  int32_t bodies_per_thread; /* mixed precision: 1 = packed f32x2 loop over pairs of
-                                partners (threads_per_cta <= 128; scalar FP32 loop at
-                                256), 2 = scalar FP32 loop with two bodies per thread
-                                (0 = 1) */
+  int32_t bodies_per_thread; /* mixed precision: 1 or 2 bodies per thread; the packed
+                                f32x2 loop over pairs of partners at threads_per_cta <= 128,
+                                the scalar FP32 loop at 256 (0 = 1) */
   int32_t grid_ctas;         /* persistent grid (0 = 8 CTAs per SM) */
 } gb_batch_tiling;
 

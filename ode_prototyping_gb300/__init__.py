@@ -263,9 +263,9 @@ def tableau(name_or_struct) -> GbTableau:
 def tiling(j_split=0, lanes=0, bodies_per_cta=0, scalar=False,
            mixed_variant=0) -> GbForceTiling:
     """Force-kernel tiling.  Mixed precision: scalar=True (or mixed_variant=1)
-    selects the scalar FP32 pair loop, mixed_variant=2 / 4 the packed f32x2
-    loop with one / two pairs of bodies per thread, 3 the packed loop with
-    one body per thread and pairs of partners, 0 the library's choice (3)."""
+    selects the scalar FP32 pair loop, mixed_variant=2 / 3 the packed f32x2
+    loop over pairs of partners with two bodies / one body per thread, 0 the
+    library's choice (2)."""
     return GbForceTiling(j_split, lanes, bodies_per_cta, 1 if scalar else mixed_variant)
 
 
@@ -601,7 +601,7 @@ class Integrator:
         n = C.c_int64(0)
         check(lib().gb_integrator_geometry(self.h, C.byref(t), C.byref(n)),
               "gb_integrator_geometry")
-        bpt = {1: 2, 2: 2, 3: 1, 4: 4}.get(t.mixed_variant, 1)
+        bpt = {1: 2, 2: 2, 3: 1}.get(t.mixed_variant, 1)
         return {"j_split": t.j_split, "lanes": t.lanes, "bodies_per_cta": t.bodies_per_cta,
                 "threads": t.bodies_per_cta * t.lanes // bpt, "mixed_variant": t.mixed_variant,
                 "ctas": int(n.value)}

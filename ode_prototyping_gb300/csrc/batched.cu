@@ -79,8 +79,8 @@ __global__ void __launch_bounds__(T)
     batch_stage_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ BatchParams P, int s) {
   constexpr int BI = (T / L) * BPT;
-  // one body per thread (T <= 128): the packed loop over pairs of partners
-  constexpr bool PK = PREC == GB_PREC_MIXED && BPT == 1 && T <= 128;
+  // T <= 128: the packed loop over pairs of partners (one or two bodies per thread)
+  constexpr bool PK = PREC == GB_PREC_MIXED && T <= 128;
   constexpr int SMEM_BODY_BYTES =
       PREC == GB_PREC_F64 ? 32 * T : (PK ? jp_smem_bytes<T>() : (int)sizeof(PackedBody) * T);
   __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(T)
         const PackedBody* src = (s == 0) ? P.PX + (long long)px * P.total_bodies + sy.body_off
                                          : P.PY + (long long)(s & 1) * P.total_bodies + sy.body_off;
         if constexpr (PK)
-          force_mixed_cta_jp<T, L>(src, n, i0, 0, n, sy.eps2f, sh_raw, part);
+          force_mixed_cta_jp<T, L, BPT>(src, n, i0, 0, n, sy.eps2f, sh_raw, part);
         else
           force_mixed_cta<T, L, BPT, true>(src, n, i0, 0, n, sy.eps2f,
                                            reinterpret_cast<PackedBody*>(sh_raw), part);
@@ -217,8 +217,8 @@ __global__ void __launch_bounds__(T)
     batch_rhs_kernel(const __grid_constant__ BatchParams P, const double* __restrict__ x,
                      const PackedBody* __restrict__ packed, double* __restrict__ out) {
   constexpr int BI = (T / L) * BPT;
-  // one body per thread (T <= 128): the packed loop over pairs of partners
-  constexpr bool PK = PREC == GB_PREC_MIXED && BPT == 1 && T <= 128;
+  // T <= 128: the packed loop over pairs of partners (one or two bodies per thread)
+  constexpr bool PK = PREC == GB_PREC_MIXED && T <= 128;
   constexpr int SMEM_BODY_BYTES =
       PREC == GB_PREC_F64 ? 32 * T : (PK ? jp_smem_bytes<T>() : (int)sizeof(PackedBody) * T);
   __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(T)
       force_f64_cta<T, L>(xs, n, i0, 0, n, sy.eps2, nullptr, sh_pos, sh_pos + 3 * T, part);
     } else {
       if constexpr (PK)
-        force_mixed_cta_jp<T, L>(packed + sy.body_off, n, i0, 0, n, sy.eps2f, sh_raw, part);
+        force_mixed_cta_jp<T, L, BPT>(packed + sy.body_off, n, i0, 0, n, sy.eps2f, sh_raw, part);
       else
         force_mixed_cta<T, L, BPT, true>(packed + sy.body_off, n, i0, 0, n, sy.eps2f,
                                          reinterpret_cast<PackedBody*>(sh_raw), part);

@@ -332,13 +332,10 @@ __device__ __forceinline__ void force_mixed_cta(const PackedBody* __restrict__ p
 }
 
 // ---------------------------------------------------------------------------
-// Packed form of force_mixed_cta for two bodies per thread and uniform
-// masses: Blackwell's f32x2 instructions (add/sub/mul/fma on a pair of FP32
-// values) carry both bodies through one instruction stream.  The j-tile is
-// staged in shared memory with every coordinate duplicated into a pair,
-// (hx,hx,hy,hy) (hz,hz,lx,lx) (ly,ly,lz,lz), so each pair operand is one
-// 64-bit register read by a vector load.  Same arithmetic per body as the
-// scalar path (the two lanes of a pair are independent IEEE operations).
+// Blackwell's packed f32x2 instructions (add/sub/mul/fma on a pair of FP32
+// values held in one 64-bit register; the two lanes are independent IEEE
+// operations).  ncu shows each holding the FMA pipe for two cycles, so they
+// save issue slots, not pipe cycles.
 // ---------------------------------------------------------------------------
 typedef unsigned long long f2_t;
 
@@ -371,175 +368,17 @@ __device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c) {
   return r;
 }
 
-// Staged j-record: three 16-byte pairs-of-pairs (48 bytes per body).
-struct __align__(16) PairRec {
-  ulonglong2 xy;  // (hx,hx), (hy,hy)
-  ulonglong2 zl;  // (hz,hz), (lx,lx)
-  ulonglong2 yz;  // (ly,ly), (lz,lz)
-};
-
-template <int T, int L, int PB>
-__device__ __forceinline__ void force_mixed_cta_x2(const PackedBody* __restrict__ packed,
-                                                   long long n, long long i0, long long jb,
-                                                   long long je, float eps2, PairRec* sh,
-                                                   double (*part)[3]) {
-  // PB pairs of bodies per thread: pair p holds bodies q = 2p and 2p + 1 of
-  // the thread's body group, i.e. i = i0 + q * BG + g.
-  constexpr int BG = T / L;
-  constexpr int NB = 2 * PB;
-  const int g = threadIdx.x / L;
-  const int l = threadIdx.x % L;
-  f2_t HX[PB], HY[PB], HZ[PB], LX[PB], LY[PB], LZ[PB];
-  int near2[NB];
-#pragma unroll
-  for (int p = 0; p < PB; ++p) {
-    PackedBody pb[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const long long i = i0 + (long long)(2 * p + h) * BG + g;
-      if (i < n) {
-        pb[h] = packed[i];
-      } else {
-        pb[h].hw = make_float4(0.f, 0.f, 0.f, 0.f);
-        pb[h].lo = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      near2[2 * p + h] = near_threshold_bits(pb[h].hw.x, pb[h].hw.y, pb[h].hw.z);
-    }
-    HX[p] = f2_pack(pb[0].hw.x, pb[1].hw.x);
-    HY[p] = f2_pack(pb[0].hw.y, pb[1].hw.y);
-    HZ[p] = f2_pack(pb[0].hw.z, pb[1].hw.z);
-    LX[p] = f2_pack(pb[0].lo.x, pb[1].lo.x);
-    LY[p] = f2_pack(pb[0].lo.y, pb[1].lo.y);
-    LZ[p] = f2_pack(pb[0].lo.z, pb[1].lo.z);
-  }
-  const f2_t E2 = f2_pack(eps2, eps2);
-  float sx[NB], sy[NB], sz[NB], cx[NB], cy[NB], cz[NB];
-#pragma unroll
-  for (int q = 0; q < NB; ++q) sx[q] = sy[q] = sz[q] = cx[q] = cy[q] = cz[q] = 0.f;
-  constexpr int JT = T;  // bodies per j-tile: one record per thread
-  // the next tile's record is loaded into registers while this tile computes
-  PackedBody nxt;
-  if (jb + threadIdx.x < je) nxt = packed[jb + threadIdx.x];
-  for (long long j0 = jb; j0 < je; j0 += JT) {
-    const int cnt = (int)min((long long)JT, je - j0);
-    __syncthreads();
-    if (threadIdx.x < cnt) {
-      PairRec r;
-      r.xy = make_ulonglong2(f2_pack(nxt.hw.x, nxt.hw.x), f2_pack(nxt.hw.y, nxt.hw.y));
-      r.zl = make_ulonglong2(f2_pack(nxt.hw.z, nxt.hw.z), f2_pack(nxt.lo.x, nxt.lo.x));
-      r.yz = make_ulonglong2(f2_pack(nxt.lo.y, nxt.lo.y), f2_pack(nxt.lo.z, nxt.lo.z));
-      sh[threadIdx.x] = r;
-    }
-    __syncthreads();
-    if (j0 + JT + threadIdx.x < je) nxt = packed[j0 + JT + threadIdx.x];
-    f2_t TX[PB], TY[PB], TZ[PB];
-#pragma unroll
-    for (int p = 0; p < PB; ++p) TX[p] = TY[p] = TZ[p] = 0ULL;  // (+0.f, +0.f)
-    // This lane's partners are jj = l + L k, k < kn.  The loop adds every
-    // pair's hi-only term without branching and marks close pairs in a
-    // 32-bit mask per chunk of 32 k; the marked pairs are then revisited:
-    // the hi-only term is taken out again and the hi/lo term added.
-    const int kn = (cnt - l + L - 1) / L;
-    for (int k0 = 0; k0 < kn; k0 += 32) {
-      const int kc = min(32, kn - k0);
-      unsigned mask = 0;
-#pragma unroll(4 / PB)
-      for (int u = 0; u < kc; ++u) {
-        const int jj = l + (k0 + u) * L;
-        const ulonglong2 xy = sh[jj].xy;
-        const f2_t hz = sh[jj].zl.x;
-        bool close = false;
-#pragma unroll
-        for (int p = 0; p < PB; ++p) {
-          const f2_t dx = f2_sub(xy.x, HX[p]);
-          const f2_t dy = f2_sub(xy.y, HY[p]);
-          const f2_t dz = f2_sub(hz, HZ[p]);
-          const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-          float ra, rb;
-          f2_unpack(r2, ra, rb);
-          close |= (__float_as_int(ra) < near2[2 * p]) | (__float_as_int(rb) < near2[2 * p + 1]);
-          const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-          const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
-          TX[p] = f2_fma(sc, dx, TX[p]);
-          TY[p] = f2_fma(sc, dy, TY[p]);
-          TZ[p] = f2_fma(sc, dz, TZ[p]);
-        }
-        mask |= (unsigned)close << u;
-      }
-      while (mask) {
-        const int u = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const int jj = l + (k0 + u) * L;
-        const ulonglong2 xy = sh[jj].xy;
-        const ulonglong2 zl = sh[jj].zl;
-        const ulonglong2 yz = sh[jj].yz;
-#pragma unroll
-        for (int p = 0; p < PB; ++p) {
-          f2_t dx = f2_sub(xy.x, HX[p]);
-          f2_t dy = f2_sub(xy.y, HY[p]);
-          f2_t dz = f2_sub(zl.x, HZ[p]);
-          f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-          float ra, rb;
-          f2_unpack(r2, ra, rb);
-          f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-          const f2_t nsc = f2_mul(f2_mul(ri, f2_mul(ri, ri)), f2_pack(-1.f, -1.f));
-          TX[p] = f2_fma(nsc, dx, TX[p]);  // take the hi-only term out again
-          TY[p] = f2_fma(nsc, dy, TY[p]);
-          TZ[p] = f2_fma(nsc, dz, TZ[p]);
-          dx = f2_add(dx, f2_sub(zl.y, LX[p]));
-          dy = f2_add(dy, f2_sub(yz.x, LY[p]));
-          dz = f2_add(dz, f2_sub(yz.y, LZ[p]));
-          r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-          f2_unpack(r2, ra, rb);
-          ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-          const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
-          TX[p] = f2_fma(sc, dx, TX[p]);
-          TY[p] = f2_fma(sc, dy, TY[p]);
-          TZ[p] = f2_fma(sc, dz, TZ[p]);
-        }
-      }
-    }
-#pragma unroll
-    for (int p = 0; p < PB; ++p) {
-      float tx[2], ty[2], tz[2];
-      f2_unpack(TX[p], tx[0], tx[1]);
-      f2_unpack(TY[p], ty[0], ty[1]);
-      f2_unpack(TZ[p], tz[0], tz[1]);
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int q = 2 * p + h;
-        kahan_add(sx[q], cx[q], tx[h]);
-        kahan_add(sy[q], cy[q], ty[h]);
-        kahan_add(sz[q], cz[q], tz[h]);
-      }
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < NB; ++q) {
-    double ax = dsub((double)sx[q], (double)cx[q]);
-    double ay = dsub((double)sy[q], (double)cy[q]);
-    double az = dsub((double)sz[q], (double)cz[q]);
-    ax = lane_reduce<L>(ax);
-    ay = lane_reduce<L>(ay);
-    az = lane_reduce<L>(az);
-    if (l == 0) {
-      part[q * BG + g][0] = ax;
-      part[q * BG + g][1] = ay;
-      part[q * BG + g][2] = az;
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
-// Packed form with one body per thread and pairs of partners: each f32x2
-// instruction carries partners j and j + 1 of the same body, so the staged
-// partner records need no duplicated coordinates and a CTA of T threads holds
-// T / L bodies (twice the warps of the two-bodies-per-thread form for the same
-// bodies, which hides more latency on small systems).  Tiles of 2T partners
-// are copied with cp.async into a double-buffered raw area (no registers held
-// across the compute loop); each thread copies two partners and builds one
-// record from them.  A missing second partner (odd tail) is placed at 1e18:
-// its r^-3 underflows to zero, so its term is exactly zero.
+// Packed loop over pairs of partners: each f32x2 instruction carries
+// partners j and j + 1 of the same body, so the staged partner records need
+// no duplicated coordinates.  NB bodies per thread (1 or 2): body q of thread
+// group g is i0 + q * (T / L) + g; with two, every 48-byte record feeds two
+// independent instruction chains (four interactions per record read).  Tiles
+// of 2T partners are copied with cp.async (no registers held across the
+// compute loop); each thread copies two partners and builds one record from
+// them.  A missing second partner (odd tail) is placed at 1e18: its r^-3
+// underflows to zero, so its term is exactly zero.  A close pair for either
+// body sends both bodies' terms of that record through the hi/lo revisit.
 // ---------------------------------------------------------------------------
 struct __align__(16) PartnerPair {
   ulonglong2 xy;  // (hx_j, hx_j+1), (hy_j, hy_j+1)
@@ -564,32 +403,41 @@ constexpr int jp_smem_bytes() {
   return 2 * (int)sizeof(PartnerPair) * T + 2 * T * (int)sizeof(PackedBody);
 }
 
-template <int T, int L>
+template <int T, int L, int NB = 1>
 __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict__ packed,
                                                    long long n, long long i0, long long jb,
                                                    long long je, float eps2, unsigned char* smem,
                                                    double (*part)[3]) {
-  constexpr int BG = T / L;  // bodies per CTA
+  constexpr int BG = T / L;  // body groups per CTA (NB bodies each)
   constexpr int JT = 2 * T;  // partners per tile
   PartnerPair* recs = reinterpret_cast<PartnerPair*>(smem);  // two buffers of T records
   PackedBody* raw = reinterpret_cast<PackedBody*>(smem + 2 * sizeof(PartnerPair) * T);
   const int g = threadIdx.x / L;
   const int l = threadIdx.x % L;
-  const long long i = i0 + g;
-  PackedBody pb;
-  if (i < n) {
-    pb = packed[i];
-  } else {
-    pb.hw = make_float4(0.f, 0.f, 0.f, 0.f);
-    pb.lo = make_float4(0.f, 0.f, 0.f, 0.f);
+  f2_t HX[NB], HY[NB], HZ[NB], LX[NB], LY[NB], LZ[NB];
+  int near2[NB];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    const long long i = i0 + (long long)q * BG + g;
+    PackedBody pb;
+    if (i < n) {
+      pb = packed[i];
+    } else {
+      pb.hw = make_float4(0.f, 0.f, 0.f, 0.f);
+      pb.lo = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    HX[q] = f2_pack(pb.hw.x, pb.hw.x);
+    HY[q] = f2_pack(pb.hw.y, pb.hw.y);
+    HZ[q] = f2_pack(pb.hw.z, pb.hw.z);
+    LX[q] = f2_pack(pb.lo.x, pb.lo.x);
+    LY[q] = f2_pack(pb.lo.y, pb.lo.y);
+    LZ[q] = f2_pack(pb.lo.z, pb.lo.z);
+    near2[q] = near_threshold_bits(pb.hw.x, pb.hw.y, pb.hw.z);
   }
-  const f2_t HX = f2_pack(pb.hw.x, pb.hw.x), HY = f2_pack(pb.hw.y, pb.hw.y),
-             HZ = f2_pack(pb.hw.z, pb.hw.z);
-  const f2_t LX = f2_pack(pb.lo.x, pb.lo.x), LY = f2_pack(pb.lo.y, pb.lo.y),
-             LZ = f2_pack(pb.lo.z, pb.lo.z);
   const f2_t E2 = f2_pack(eps2, eps2);
-  const int near2 = near_threshold_bits(pb.hw.x, pb.hw.y, pb.hw.z);
-  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  float sx[NB], sy[NB], sz[NB], cx[NB], cy[NB], cz[NB];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) sx[q] = sy[q] = sz[q] = cx[q] = cy[q] = cz[q] = 0.f;
   // Thread t copies partners j0 + 2t and j0 + 2t + 1 of every tile into its
   // own two raw slots and later builds record t from them, so the single raw
   // area needs no barrier: a thread re-issues its slots only after reading
@@ -638,32 +486,40 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     const int cnt = (int)min((long long)JT, je - j0);
     const int npair = (cnt + 1) / 2;
     const PartnerPair* rec = recs + buf * T;
-    f2_t TX = 0ULL, TY = 0ULL, TZ = 0ULL;
+    f2_t TX[NB], TY[NB], TZ[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) TX[q] = TY[q] = TZ[q] = 0ULL;
+    // This lane's records are jj = l + L k, k < kn.  Every pair's hi-only term
+    // is added without branching; a record with a close pair (the smaller r^2
+    // bit pattern below the body's threshold) is marked by shifting a bit into
+    // a 32-bit mask per chunk of 32 k (bit b is iteration kc - 1 - b), and the
+    // marked records are revisited: hi-only terms out, hi/lo terms in.
     const int kn = (npair - l + L - 1) / L;
     for (int k0 = 0; k0 < kn; k0 += 32) {
       const int kc = min(32, kn - k0);
       unsigned mask = 0;
-#pragma unroll 4
+#pragma unroll(4 / NB)
       for (int u = 0; u < kc; ++u) {
         const int jj = l + (k0 + u) * L;
         const ulonglong2 xy = rec[jj].xy;
         const f2_t hz = rec[jj].zl.x;
-        const f2_t dx = f2_sub(xy.x, HX);
-        const f2_t dy = f2_sub(xy.y, HY);
-        const f2_t dz = f2_sub(hz, HZ);
-        const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-        float ra, rb;
-        f2_unpack(r2, ra, rb);
-        // both partners share the body's threshold: one comparison of the
-        // smaller bit pattern, shifted in (bit b of the chunk's mask is
-        // iteration kc - 1 - b)
-        mask = (mask << 1) |
-               (unsigned)(min(__float_as_int(ra), __float_as_int(rb)) < near2);
-        const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-        const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
-        TX = f2_fma(sc, dx, TX);
-        TY = f2_fma(sc, dy, TY);
-        TZ = f2_fma(sc, dz, TZ);
+        bool close = false;
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+          const f2_t dx = f2_sub(xy.x, HX[q]);
+          const f2_t dy = f2_sub(xy.y, HY[q]);
+          const f2_t dz = f2_sub(hz, HZ[q]);
+          const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+          float ra, rb;
+          f2_unpack(r2, ra, rb);
+          close |= min(__float_as_int(ra), __float_as_int(rb)) < near2[q];
+          const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+          const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+          TX[q] = f2_fma(sc, dx, TX[q]);
+          TY[q] = f2_fma(sc, dy, TY[q]);
+          TZ[q] = f2_fma(sc, dz, TZ[q]);
+        }
+        mask = (mask << 1) | (unsigned)close;
       }
       while (mask) {
         const int u = kc - __ffs(mask);
@@ -672,39 +528,45 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
         const ulonglong2 xy = rec[jj].xy;
         const ulonglong2 zl = rec[jj].zl;
         const ulonglong2 yz = rec[jj].yz;
-        f2_t dx = f2_sub(xy.x, HX);
-        f2_t dy = f2_sub(xy.y, HY);
-        f2_t dz = f2_sub(zl.x, HZ);
-        f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-        float ra, rb;
-        f2_unpack(r2, ra, rb);
-        f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-        const f2_t nsc = f2_mul(f2_mul(ri, f2_mul(ri, ri)), f2_pack(-1.f, -1.f));
-        TX = f2_fma(nsc, dx, TX);  // take the hi-only terms out again
-        TY = f2_fma(nsc, dy, TY);
-        TZ = f2_fma(nsc, dz, TZ);
-        dx = f2_add(dx, f2_sub(zl.y, LX));
-        dy = f2_add(dy, f2_sub(yz.x, LY));
-        dz = f2_add(dz, f2_sub(yz.y, LZ));
-        r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
-        f2_unpack(r2, ra, rb);
-        ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
-        const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
-        TX = f2_fma(sc, dx, TX);
-        TY = f2_fma(sc, dy, TY);
-        TZ = f2_fma(sc, dz, TZ);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+          f2_t dx = f2_sub(xy.x, HX[q]);
+          f2_t dy = f2_sub(xy.y, HY[q]);
+          f2_t dz = f2_sub(zl.x, HZ[q]);
+          f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+          float ra, rb;
+          f2_unpack(r2, ra, rb);
+          f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+          const f2_t nsc = f2_mul(f2_mul(ri, f2_mul(ri, ri)), f2_pack(-1.f, -1.f));
+          TX[q] = f2_fma(nsc, dx, TX[q]);
+          TY[q] = f2_fma(nsc, dy, TY[q]);
+          TZ[q] = f2_fma(nsc, dz, TZ[q]);
+          dx = f2_add(dx, f2_sub(zl.y, LX[q]));
+          dy = f2_add(dy, f2_sub(yz.x, LY[q]));
+          dz = f2_add(dz, f2_sub(yz.y, LZ[q]));
+          r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+          f2_unpack(r2, ra, rb);
+          ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+          const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+          TX[q] = f2_fma(sc, dx, TX[q]);
+          TY[q] = f2_fma(sc, dy, TY[q]);
+          TZ[q] = f2_fma(sc, dz, TZ[q]);
+        }
       }
     }
-    float t0, t1;
-    f2_unpack(TX, t0, t1);
-    kahan_add(sx, cx, t0);
-    kahan_add(sx, cx, t1);
-    f2_unpack(TY, t0, t1);
-    kahan_add(sy, cy, t0);
-    kahan_add(sy, cy, t1);
-    f2_unpack(TZ, t0, t1);
-    kahan_add(sz, cz, t0);
-    kahan_add(sz, cz, t1);
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      float t0, t1;
+      f2_unpack(TX[q], t0, t1);
+      kahan_add(sx[q], cx[q], t0);
+      kahan_add(sx[q], cx[q], t1);
+      f2_unpack(TY[q], t0, t1);
+      kahan_add(sy[q], cy[q], t0);
+      kahan_add(sy[q], cy[q], t1);
+      f2_unpack(TZ[q], t0, t1);
+      kahan_add(sz[q], cz[q], t0);
+      kahan_add(sz[q], cz[q], t1);
+    }
     if (j0 + JT < je) {
       cp_async_wait_all();                 // this thread's copies of tile k + 1
       build(j0 + JT, recs + (buf ^ 1) * T);
@@ -712,16 +574,19 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     }
     __syncthreads();
   }
-  double ax = dsub((double)sx, (double)cx);
-  double ay = dsub((double)sy, (double)cy);
-  double az = dsub((double)sz, (double)cz);
-  ax = lane_reduce<L>(ax);
-  ay = lane_reduce<L>(ay);
-  az = lane_reduce<L>(az);
-  if (l == 0) {
-    part[g][0] = ax;
-    part[g][1] = ay;
-    part[g][2] = az;
+#pragma unroll
+  for (int q = 0; q < NB; ++q) {
+    double ax = dsub((double)sx[q], (double)cx[q]);
+    double ay = dsub((double)sy[q], (double)cy[q]);
+    double az = dsub((double)sz[q], (double)cz[q]);
+    ax = lane_reduce<L>(ax);
+    ay = lane_reduce<L>(ay);
+    az = lane_reduce<L>(az);
+    if (l == 0) {
+      part[q * BG + g][0] = ax;
+      part[q * BG + g][1] = ay;
+      part[q * BG + g][2] = az;
+    }
   }
 }
 
@@ -885,17 +750,17 @@ __device__ __forceinline__ PackedBody pack_body(double x, double y, double z, do
 }
 
 // Launch geometry shared by the standalone and fused kernels.
-// Mixed pair loop used when the tiling leaves the choice open (1 scalar,
-// 2 / 4 packed with one / two pairs of bodies per thread, 3 packed with one
-// body per thread and pairs of partners).
-constexpr int kDefaultMixedVariant = 3;
+// Mixed pair loop used when the tiling leaves the choice open: 1 scalar FP32
+// (two bodies per thread), 2 / 3 packed f32x2 over pairs of partners with two
+// bodies / one body per thread.
+constexpr int kDefaultMixedVariant = 2;
 
 struct ForceGeom {
   int T;      // threads per CTA
   int L;      // lanes per body
   int P;      // cluster size
   int BPT;    // bodies per thread (mixed path)
-  int variant;  // mixed pair loop: 1 scalar, 2 / 4 packed with 1 / 2 pairs per thread
+  int variant;  // mixed pair loop: 1 scalar, 2 / 3 packed with two bodies / one body per thread
   long long n_itiles;
   int bodies_per_cta() const { return (T / L) * BPT; }
 };

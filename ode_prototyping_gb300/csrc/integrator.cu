@@ -36,15 +36,14 @@ size_t norm_workspace_bytes(long long n);
 namespace {
 
 template <int PREC, int T, int L, int BPT, bool PACKED = false>
-__global__ void __launch_bounds__(T, PACKED && BPT <= 2 ? 7 * 128 / T : (PACKED ? 4 * 128 / T : 5 * 128 / T))
+__global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 5 * 128 / T)
     fused_stage_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ FusedParams P, int s) {
   constexpr int BI = (T / L) * BPT;
   constexpr int SMEM_BODY_BYTES =
       PREC == GB_PREC_F64
           ? 32 * T
-          : (PACKED ? (BPT == 1 ? jp_smem_bytes<T>() : (int)sizeof(PairRec) * T)
-                    : (int)sizeof(PackedBody) * T);
+          : (PACKED ? jp_smem_bytes<T>() : (int)sizeof(PackedBody) * T);
   __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
   __shared__ double part[BI][3];
   __shared__ double red[T];
@@ -71,11 +70,9 @@ __global__ void __launch_bounds__(T, PACKED && BPT <= 2 ? 7 * 128 / T : (PACKED 
       force_f64_cta<T, L>(ysrc, n, i0, jb, je, P.eps2, P.masses, sh_pos, sh_m, part);
     } else {
       const PackedBody* src = (s == 0) ? P.PX + (long long)px * n : P.PY + (long long)(s & 1) * n;
-      if constexpr (PACKED && BPT == 1) {
-        force_mixed_cta_jp<T, L>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
-      } else if constexpr (PACKED) {
-        force_mixed_cta_x2<T, L, BPT / 2>(src, n, i0, jb, je, P.eps2f,
-                                          reinterpret_cast<PairRec*>(sh_raw), part);
+      if constexpr (PACKED) {
+        static_assert(BPT == 1 || BPT == 2, "packed loop: one or two bodies per thread");
+        force_mixed_cta_jp<T, L, BPT>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
       } else if (P.masses) {
         force_mixed_cta<T, L, BPT, false>(src, n, i0, jb, je, P.eps2f,
                                           reinterpret_cast<PackedBody*>(sh_raw), part);
@@ -497,8 +494,6 @@ const void* pick_fused(int prec, int T, int L, int BPT, bool packed = false) {
   if (prec == GB_PREC_MIXED && packed) {
     if (T == 128 && BPT == 1) return pick_packed<128, 1>(L);
     if (T == 128 && BPT == 2) return pick_packed<128, 2>(L);
-    if (T == 128 && BPT == 4) return pick_packed<128, 4>(L);
-    if (T == 256 && BPT == 2) return pick_packed<256, 2>(L);
     return nullptr;
   }
   if (prec == GB_PREC_F64) {

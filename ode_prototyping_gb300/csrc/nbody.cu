@@ -89,20 +89,16 @@ __global__ void __launch_bounds__(T) rhs_mixed_kernel(const PackedBody* __restri
                                                       long long n, float eps2, double mass,
                                                       int uniform_mass) {
   constexpr int BI = (T / L) * BPT;
-  constexpr int SH = PACKED ? (BPT == 1 ? jp_smem_bytes<T>() : (int)sizeof(PairRec) * T)
-                            : (int)sizeof(PackedBody) * T;
+  constexpr int SH = PACKED ? jp_smem_bytes<T>() : (int)sizeof(PackedBody) * T;
   __shared__ __align__(16) unsigned char sh_raw[SH];
   __shared__ double part[BI][3];
   const ClusterInfo ci = cluster_info();
   const long long i0 = ci.itile * BI;
   long long jb, je;
   j_chunk(n, ci.rank, ci.size, T, jb, je);
-  if constexpr (PACKED && BPT == 1) {
-    force_mixed_cta_jp<T, L>(packed, n, i0, jb, je, eps2, sh_raw, part);
-  } else if constexpr (PACKED) {
-    static_assert(BPT == 2 || BPT == 4, "packed path carries one or two pairs per thread");
-    force_mixed_cta_x2<T, L, BPT / 2>(packed, n, i0, jb, je, eps2,
-                                      reinterpret_cast<PairRec*>(sh_raw), part);
+  if constexpr (PACKED) {
+    static_assert(BPT == 1 || BPT == 2, "packed loop: one or two bodies per thread");
+    force_mixed_cta_jp<T, L, BPT>(packed, n, i0, jb, je, eps2, sh_raw, part);
   } else {
     PackedBody* sh = reinterpret_cast<PackedBody*>(sh_raw);
     if (uniform_mass)
@@ -147,13 +143,11 @@ const void* pick_mixed_L(int L) {
 // packed: the f32x2 path (pairs of bodies per thread, uniform masses)
 template <int T>
 const void* pick_mixed(int L, int BPT, bool packed = false) {
-  if (packed && BPT == 1) return pick_mixed_L<T, 1, true>(L);
-  if (packed && BPT == 2) return pick_mixed_L<T, 2, true>(L);
-  if (packed && BPT == 4) return pick_mixed_L<T, 4, true>(L);
+  if (packed && T <= 128 && BPT == 1) return pick_mixed_L<T, 1, true>(L);
+  if (packed && T <= 128 && BPT == 2) return pick_mixed_L<T, 2, true>(L);
   switch (BPT) {
     case 1: return pick_mixed_L<T, 1, false>(L);
     case 2: return pick_mixed_L<T, 2, false>(L);
-    case 4: return pick_mixed_L<T, 4, false>(L);
     default: return nullptr;
   }
 }
@@ -161,8 +155,7 @@ const void* pick_mixed(int L, int BPT, bool packed = false) {
 // The packed loops run for uniform masses unless the tiling asks for the
 // scalar loop (mixed_variant == 1).
 bool use_packed(const gb_force_tiling* tiling, int BPT, const double* masses) {
-  return (BPT == 1 || BPT == 2 || BPT == 4) && !masses &&
-         !(tiling && tiling->mixed_variant == 1);
+  return (BPT == 1 || BPT == 2) && !masses && !(tiling && tiling->mixed_variant == 1);
 }
 
 int validate_nbody(const void* a, const void* b, long long n, double softening, double mass,
@@ -276,10 +269,10 @@ ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling,
     g.L = L;
   } else {
     int v = tiling ? tiling->mixed_variant : 0;
-    if (v < 1 || v > 4) v = kDefaultMixedVariant;
+    if (v < 1 || v > 3) v = kDefaultMixedVariant;
     if (!uniform_masses) v = 1;
     g.variant = v;
-    g.BPT = v == 4 ? 4 : (v == 3 ? 1 : 2);
+    g.BPT = v == 3 ? 1 : 2;
     // ~32 warps' worth of two-body threads per SM, each lane pair-loop at
     // least ~256 partners long; lanes only when the cluster split leaves the
     // grid well short of that (measured with the partner-pair loop: N = 4096
@@ -303,6 +296,8 @@ ForceGeom choose_geom(long long n, int precision, const gb_force_tiling* tiling,
       g.T = t <= 64 ? 64 : (t <= 128 ? 128 : 256);
     }
   }
+  // the packed loops stage 2T partners per tile: 128 threads per CTA
+  if (precision == GB_PREC_MIXED && g.variant != 1 && !exact) g.T = 128;
   const long long per_cta = g.bodies_per_cta();
   g.n_itiles = (n + per_cta - 1) / per_cta;
   return g;

@@ -115,7 +115,7 @@ def test_vector_tolerances_match_scalar(gb, torch_cuda):
     np.testing.assert_array_equal(np.array(o1.states()), np.array(o2.states()))
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 def test_mixed_precision_integrator(gb, torch_cuda, variant):
     """Every mixed pair loop (auto, scalar, one or two packed pairs per
     thread) tracks the FP64 path."""

@@ -89,7 +89,7 @@ def test_acc_write_and_accumulate(gb, orc, torch_cuda):
     np.testing.assert_array_equal(acc.cpu().numpy(), 2 * ref)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("n,soft,gen", [(1024, 0.01, "ball"), (4096, 0.005, "plummer"),
                                         (16384, 0.005, "plummer"), (3001, 0.003, "binary"),
                                         (8192, 0.002, "cold"), (7, 0.05, "plummer"),
