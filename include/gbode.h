@@ -107,7 +107,7 @@ typedef struct {
                             (0 = auto; 16 is a non-portable cluster size) */
   int32_t lanes;         /* lanes per body inside a warp: 1,2,4,8 (0 = auto) */
   int32_t bodies_per_cta;/* i-bodies per CTA: 32..256 (0 = auto) */
-  int32_t mixed_variant; /* mixed-precision pair loop: 0 = auto (2), 1 = scalar FP32 (two
+  int32_t mixed_variant; /* mixed-precision pair loop: 0 = auto (3), 1 = scalar FP32 (two
                             bodies per thread, any masses), 2 = packed f32x2 over pairs of
                             partners with two bodies per thread, 3 = the same with one
                             body per thread; the packed loops need uniform masses

@@ -265,7 +265,7 @@ def tiling(j_split=0, lanes=0, bodies_per_cta=0, scalar=False,
     """Force-kernel tiling.  Mixed precision: scalar=True (or mixed_variant=1)
     selects the scalar FP32 pair loop, mixed_variant=2 / 3 the packed f32x2
     loop over pairs of partners with two bodies / one body per thread, 0 the
-    library's choice (2)."""
+    library's choice (3)."""
     return GbForceTiling(j_split, lanes, bodies_per_cta, 1 if scalar else mixed_variant)
 
 

@@ -753,7 +753,7 @@ __device__ __forceinline__ PackedBody pack_body(double x, double y, double z, do
 // Mixed pair loop used when the tiling leaves the choice open: 1 scalar FP32
 // (two bodies per thread), 2 / 3 packed f32x2 over pairs of partners with two
 // bodies / one body per thread.
-constexpr int kDefaultMixedVariant = 2;
+constexpr int kDefaultMixedVariant = 3;
 
 struct ForceGeom {
   int T;      // threads per CTA
