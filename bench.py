@@ -288,6 +288,8 @@ def main():
     ap.add_argument("--controller", default="reference", choices=["reference", "pi", "learned"])
     ap.add_argument("--mlp", default=None, help="trained proposer weights (learned controller)")
     ap.add_argument("--n-bodies", type=int, default=16384, help="stage: bodies")
+    ap.add_argument("--stage-precision", default="mixed", choices=["mixed", "f64"],
+                    help="stage: precision of the integrator")
     ap.add_argument("--tol", type=float, default=1e-9, help="c2_tol: atol = rtol")
     ap.add_argument("--learned-config", default="plummer4096_rkf78",
                     help="c4: proposer training/evaluation configuration")
@@ -615,7 +617,7 @@ def run_other_workload(args):
         n = args.n_bodies
         x0 = gb.to_device(gb.ic_plummer(n, WORKLOAD["seed"], 1.0))
         it = gb.Integrator(WORKLOAD["tableau"], gb.NBodyODE(n, WORKLOAD["softening"], 1.0 / n),
-                           gb.Gb300Executor(precision="mixed", attempts_per_sync=1),
+                           gb.Gb300Executor(precision=args.stage_precision, attempts_per_sync=1),
                            stream=stream)
         it.start(x0, WORKLOAD["t0"], WORKLOAD["tf"], WORKLOAD["atol"], WORKLOAD["rtol"])
         ms, _ = _timed(torch, stream, lambda: it.launch_stage(1), 1, flush)
@@ -624,9 +626,11 @@ def run_other_workload(args):
                 it.launch_stage(2 + r)
         stream.synchronize()
         line.update(metric="fused stage kernel, one launch", unit="ms", value=ms,
-                    higher_is_better=False, dtype="f32+f64", steps=1, ms_per_step=ms,
+                    higher_is_better=False, steps=1, ms_per_step=ms,
+                    dtype="f32+f64" if args.stage_precision == "mixed" else "f64",
                     geometry=it.geometry(),
-                    config={"workload": f"plummer{n}_rkf78_mixed_stage", "n_particles": n,
+                    config={"workload": f"plummer{n}_rkf78_{args.stage_precision}_stage",
+                            "n_particles": n,
                             "step": "one fused stage launch (four launched)"})
         it.close()
     elif args.workload == "c4":
