@@ -113,3 +113,28 @@ def test_batch_learned_controller(gb, torch_cuda):
 def test_batch_learned_requires_network(gb, torch_cuda):
     with pytest.raises(gb.GbError):
         gb.Batch("DOPRI5", [32], 0.05, precision="f64", controller="learned")
+
+
+def test_batch_pi_controller_matches_single_system(gb, torch_cuda):
+    """The PI controller in the batch's per-system control warp takes the same
+    accepted steps as the single-system integrator's PI controller."""
+    sizes = [40, 90, 150]
+    soft, tol, tf = 0.05, 1e-9, 0.1
+    xs, x0 = _systems(gb, sizes, 80)
+    b = gb.Batch("DOPRI5", sizes, soft, precision="f64", controller="pi")
+    b.start(x0, 0.0, tf, tol, tol)
+    assert b.advance() == 0
+    st = b.stats(per_system=True)
+    x, t = b.state()
+    x = x.cpu().numpy()
+    np.testing.assert_allclose(t, tf)
+    for k, n in enumerate(sizes):
+        it = gb.Integrator("DOPRI5", gb.NBodyODE(n, soft, 1.0 / n),
+                           gb.Gb300Executor(precision="f64", controller="pi"))
+        it.start(xs[k], 0.0, tf, tol, tol)
+        assert it.advance(0) == 0
+        assert abs(st["systems"][k]["n_accepted"] - it.stats()["n_accepted"]) <= 1, k
+        xk, _ = it.state()
+        assert np.max(np.abs(b.system_state(x, k) - xk.cpu().numpy())) <= 10 * tol
+        it.close()
+    b.close()

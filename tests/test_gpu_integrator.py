@@ -232,3 +232,40 @@ def test_dopri5_dense_output(gb, torch_cuda):
         k = int(np.where(np.array(out.times()) == t)[0][0])
         j = int(np.where(times == t)[0][0])
         np.testing.assert_allclose(dense[j], states[k], rtol=0, atol=1e-13)
+
+
+def test_mixed_integrator_per_body_masses(gb, torch_cuda):
+    """Per-body masses run the scalar FP32 pair loop in the mixed path; the
+    integration tracks the FP64 path with the same masses."""
+    n = 700
+    x0 = gb.ic_plummer(n, 31)
+    m = np.random.default_rng(6).uniform(0.5, 1.5, n)
+    m /= m.sum()
+    md = gb.to_device(m)
+    tol = 1e-9
+    ode = gb.NBodyODE(n, 0.02, masses=md)
+    out64, outmx = gb.RawOutput(), gb.RawOutput()
+    gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, 0.1, tol, tol, ode, out64,
+                                              gb.Gb300Executor(precision="f64"))
+    gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, 0.1, tol, tol, ode, outmx,
+                                              gb.Gb300Executor(precision="mixed"))
+    assert abs(len(outmx.times()) - len(out64.times())) <= 2
+    assert np.max(np.abs(np.array(outmx.states()[-1]) - np.array(out64.states()[-1]))) <= 1e-6
+
+
+def test_dopri5_dense_output_mixed(gb, torch_cuda):
+    """Dense output in mixed precision agrees with the FP64 path's."""
+    n, soft, tol, tf = 512, 0.02, 1e-9, 0.1
+    x0 = gb.ic_plummer(n, 22)
+    ode = gb.NBodyODE(n, soft, 1.0 / n)
+    times = np.linspace(0.01, 0.09, 9)
+    dense = {}
+    for prec in ("f64", "mixed"):
+        it = gb.Integrator("DOPRI5", ode, gb.Gb300Executor(precision=prec, attempts_per_sync=4))
+        it.set_dense_output(times)
+        it.start(x0, 0.0, tf, tol, tol)
+        assert it.advance(0) == 0
+        dense[prec] = it.dense_output()
+        it.close()
+    assert dense["mixed"].shape == (len(times), 6 * n)
+    assert np.max(np.abs(dense["mixed"] - dense["f64"])) <= 1e-6

@@ -120,3 +120,17 @@ def test_leapfrog_matches_oracle(gb, orc, torch_cuda, tile, exact):
     else:
         assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1.0)) <= 1e-12
     np.testing.assert_array_equal(np.array(out.states()[-1]), got)
+
+
+def test_leapfrog_mixed_tracks_f64(gb, torch_cuda):
+    """Leapfrog on the mixed-precision force kernels stays within 1e-6 of the
+    FP64 leapfrog over 50 steps."""
+    n, soft, dt = 1024, 0.01, 1e-3
+    x0 = gb.ic_plummer(n, 18)
+    ode = gb.NBodyODE(n, soft, 1.0 / n)
+    x64, s64 = gb.ParallelLeapfrogIntegrator.integrate(x0, 0.0, 0.05, dt, ode, None,
+                                                       gb.Gb300Executor(precision="f64"))
+    xmx, smx = gb.ParallelLeapfrogIntegrator.integrate(x0, 0.0, 0.05, dt, ode, None,
+                                                       gb.Gb300Executor(precision="mixed"))
+    assert s64 == smx
+    assert (xmx - x64).abs().max().item() <= 1e-6
