@@ -632,7 +632,7 @@ extern "C" int gb_batch_create(const gb_tableau* tab, int32_t n_sys, const int64
   };
   std::vector<int> body_sys;
   for (int k = 0; k < n_sys; ++k) {
-    if (b->n[k] < 2 || !(b->soft[k] >= 0.0) || !(b->mass[k] > 0.0))
+    if (b->n[k] < 1 || !(b->soft[k] >= 0.0) || !(b->mass[k] > 0.0))
       return fail(GB_ERR_INVALID_ARGUMENT);
     if (opts.precision == GB_PREC_MIXED && !(b->soft[k] > 0.0)) return fail(GB_ERR_INVALID_ARGUMENT);
     b->total_bodies += b->n[k];

@@ -734,7 +734,7 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   if (!out) return GB_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   GB_TRY(check_tableau(tab));
-  if (!sys || sys->n_particles < 2 || !(sys->softening >= 0.0)) return GB_ERR_INVALID_ARGUMENT;
+  if (!sys || sys->n_particles < 1 || !(sys->softening >= 0.0)) return GB_ERR_INVALID_ARGUMENT;
   if (!sys->masses_dev && !(sys->mass > 0.0)) return GB_ERR_INVALID_ARGUMENT;
   gb_integrate_opts opts;
   std::memset(&opts, 0, sizeof opts);

@@ -269,3 +269,16 @@ def test_dopri5_dense_output_mixed(gb, torch_cuda):
         it.close()
     assert dense["mixed"].shape == (len(times), 6 * n)
     assert np.max(np.abs(dense["mixed"] - dense["f64"])) <= 1e-6
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_single_body_moves_uniformly(gb, torch_cuda, precision):
+    """A lone body has zero acceleration: the integrator carries it along its
+    velocity to tf."""
+    x0 = np.array([0.1, -0.2, 0.3, 0.5, 0.25, -1.0])
+    out = gb.RawOutput()
+    gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, 1.0, 1e-9, 1e-9, gb.NBodyODE(1, 0.05, 1.0),
+                                              out, gb.Gb300Executor(precision=precision))
+    xf = np.array(out.states()[-1])
+    np.testing.assert_allclose(xf[:3], x0[:3] + x0[3:], rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(xf[3:], x0[3:])

@@ -181,3 +181,25 @@ def test_rhs_mixed_sorted_masses_and_displaced(gb, torch_cuda):
     xs[: 3 * n] += 1.0e4
     got2 = gb.nbody_rhs_mixed_sorted(xs, n, 0.01, masses=mt).cpu().numpy()
     assert _rel(got2[3 * n:], ref[3 * n:]) <= 2e-6
+
+
+@pytest.mark.parametrize("n", [1, 2, 3])
+def test_tiny_systems_both_precisions(gb, orc, torch_cuda, n):
+    """Edge sizes: a lone body feels no force (its self-pair contributes an
+    exact zero); two and three bodies match the oracle."""
+    x = _x(n, 40 + n)
+    ode, _ = orc.nbody_ode(n, 0.05, 1.0 / n)
+    ref = orc.rhs(ode, x)
+    got64 = gb.nbody_rhs_f64(x, n, 0.05, 1.0 / n, tile=gb.tiling(1, 1, 0)).cpu().numpy()
+    np.testing.assert_array_equal(got64, ref)
+    gotmx = gb.nbody_rhs_mixed(x, n, 0.05, 1.0 / n).cpu().numpy()
+    np.testing.assert_array_equal(gotmx[: 3 * n], ref[: 3 * n])
+    if n == 1:
+        assert np.all(gotmx[3:] == 0.0)
+    else:
+        assert _rel(gotmx[3 * n:], ref[3 * n:]) <= 1e-6
+
+
+def test_empty_system_rejected(gb, torch_cuda):
+    with pytest.raises(gb.GbError):
+        gb.nbody_rhs_f64(np.zeros(0), 0, 0.05, 1.0)
