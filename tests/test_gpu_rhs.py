@@ -203,3 +203,21 @@ def test_tiny_systems_both_precisions(gb, orc, torch_cuda, n):
 def test_empty_system_rejected(gb, torch_cuda):
     with pytest.raises(gb.GbError):
         gb.nbody_rhs_f64(np.zeros(0), 0, 0.05, 1.0)
+
+
+def test_rhs_mixed_large_system_properties(gb, torch_cuda):
+    """Full-size check at N = 131072 (cold collapse, eps = 0.002): the mixed
+    accelerations stay within 1e-6 of FP64 normwise, and the total force
+    vanishes (pair terms are antisymmetric) to FP32 summation accuracy."""
+    torch = torch_cuda
+    n, soft = 131072, 0.002
+    x = gb.ic_cold_sphere(n, 9, 0.01)
+    ref = gb.nbody_rhs_f64(x, n, soft, 1.0 / n)
+    got = gb.nbody_rhs_mixed(x, n, soft, 1.0 / n)
+    a64 = ref[3 * n:].view(-1, 3)
+    amx = got[3 * n:].view(-1, 3)
+    rel = ((amx - a64).norm() / a64.norm()).item()
+    assert rel <= 1e-6, rel
+    net = amx.sum(0).norm().item() / amx.norm(dim=1).sum().item()
+    assert net <= 1e-6, net
+    assert torch.equal(got[: 3 * n], ref[: 3 * n])
