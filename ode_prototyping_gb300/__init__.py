@@ -467,6 +467,7 @@ class Gb300Executor:
     mlp: GbMlp | None = None
     log_steps: int = 0
     spatial_sort: bool = False
+    host_wait_timeout_s: float = 600.0  # bound on each host wait for the device
 
     def rhs(self, ode: NBodyODE, x, dxdt):
         if self.precision == "f64":
@@ -485,7 +486,7 @@ class Gb300Executor:
         o.attempts_per_sync = self.attempts_per_sync
         o.record = 1 if record else 0
         o.max_attempts = self.max_attempts
-        o.host_wait_timeout_s = 600.0
+        o.host_wait_timeout_s = self.host_wait_timeout_s
         o.pi_beta = self.pi_beta
         if self.tile is not None:
             o.tiling = self.tile

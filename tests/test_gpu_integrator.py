@@ -282,3 +282,18 @@ def test_single_body_moves_uniformly(gb, torch_cuda, precision):
     xf = np.array(out.states()[-1])
     np.testing.assert_allclose(xf[:3], x0[:3] + x0[3:], rtol=0, atol=1e-12)
     np.testing.assert_array_equal(xf[3:], x0[3:])
+
+
+def test_bounded_host_wait_times_out(gb, torch_cuda):
+    """Every host wait for the device is bounded: a graph replay of 16 FP64
+    RKF78 attempts at N = 8192 (over a second of device work) with a 1 ms
+    bound returns GB_ERR_TIMEOUT instead of blocking, and the integrator can
+    still be closed (the failure is made on the host; nothing faults)."""
+    n = 8192
+    x0 = gb.ic_plummer(n, 12)
+    exe = gb.Gb300Executor(precision="f64", attempts_per_sync=16, host_wait_timeout_s=1e-3)
+    it = gb.Integrator("RKF78", gb.NBodyODE(n, 0.005, 1.0 / n), exe)
+    it.start(x0, 0.0, 2.0, 1e-8, 1e-8)
+    assert it.advance(0) == gb.GB_ERR_TIMEOUT
+    it.close()
+    torch_cuda.cuda.synchronize()
