@@ -188,6 +188,133 @@ __device__ __forceinline__ void body_epilogue(const EpiCtx& E, long long i, cons
   }
 }
 
+// The same work for rows [b_lo, b_hi) of an i-tile, one state element per
+// thread instead of one body per thread: the rows' 3*cnt position elements
+// and 3*cnt velocity elements are contiguous in the state, so a 16-row
+// cluster slice runs its FP64 stage sums on three full warps with coalesced
+// loads, where the body form keeps one half-warp busy for six elements
+// (FP64 issues at 1/64 of the FP32 rate on this part, and the epilogue runs
+// after every CTA's pair loop, where nothing hides it).  Each element's
+// arithmetic is body_epilogue's, term for term and in the same order; only
+// the per-thread grouping of the squares in sq_acc differs.  part[b] holds
+// the cluster's pair sums on entry; on return it holds the new positions.
+// Every thread of the CTA must call it (it synchronises the CTA).
+template <int PREC, int T>
+__device__ __forceinline__ void rows_epilogue(const EpiCtx& E, long long i0, int b_lo, int b_hi,
+                                              double (*part)[3], double& sq_acc, double& amax) {
+  const DevTableau& tab = *E.tab;
+  const int s = E.s, S = E.S;
+  const long long n = E.n;
+  const int cnt = b_hi > b_lo ? b_hi - b_lo : 0;
+  const int h3 = 3 * cnt, ne = 6 * cnt;
+  const long long base = 3 * (i0 + b_lo);  // first position element of the rows
+  double* ks_s = E.ks + (long long)kslot(s, S, E.k0slot) * E.kstride;
+  if (!E.skip_force) {
+    // k_s = (v, a): velocities of the stage state, scaled pair sums
+#pragma unroll 1
+    for (int v = threadIdx.x; v < ne; v += T) {
+      double k;
+      long long idx;
+      if (v < h3) {
+        idx = base + v;
+        k = E.ysrc[3 * n + idx];
+      } else {
+        const int w = v - h3;
+        idx = 3 * n + base + w;
+        const double a = part[b_lo + w / 3][w % 3];
+        k = E.masses ? a : dmul(a, E.mass);
+      }
+      ks_s[idx] = k;
+    }
+    if (E.last) {
+#pragma unroll 1
+      for (int r = threadIdx.x; r < cnt; r += T) {
+        const double* a = part[b_lo + r];
+        double k[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) k[c] = E.masses ? a[c] : dmul(a[c], E.mass);
+        amax = fmax(amax, sqrt(k[0] * k[0] + k[1] * k[1] + k[2] * k[2]));
+      }
+    }
+  }
+  __syncthreads();  // part is read; the k_s writes are visible to the CTA
+#pragma unroll 1
+  for (int v = threadIdx.x; v < ne; v += T) {
+    const bool pos = v < h3;
+    const int w = pos ? v : v - h3;
+    const long long idx = (pos ? 0 : 3 * n) + base + w;
+    const double x0e = E.x0[idx];
+    double out;
+    if (!E.last) {
+      // terms in groups of four: a group's loads are in flight together,
+      // the sum still runs in stage order
+      const unsigned m = tab.anz[s];
+      double acc = 0.0;
+#pragma unroll 1
+      for (int l0 = 0; l0 <= s; l0 += 4) {
+        double kl[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int l = l0 + u;
+          if (l <= s && ((m >> l) & 1u)) kl[u] = E.ks[(long long)kslot(l, S, E.k0slot) * E.kstride + idx];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int l = l0 + u;
+          if (l <= s && ((m >> l) & 1u)) acc = dadd(acc, dmul(tab.a[s][l], kl[u]));
+        }
+      }
+      out = dadd(x0e, dmul(acc, E.dt));
+      E.ynext[idx] = out;
+    } else {
+      const unsigned m = tab.bnz | tab.dbnz;
+      double xv = 0.0, ev = 0.0;
+#pragma unroll 1
+      for (int l0 = 0; l0 < S; l0 += 4) {
+        double kl[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int l = l0 + u;
+          if (l < S && ((m >> l) & 1u)) kl[u] = E.ks[(long long)kslot(l, S, E.k0slot) * E.kstride + idx];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int l = l0 + u;
+          if (l >= S) break;
+          if ((tab.bnz >> l) & 1u) xv = dadd(xv, dmul(tab.b[l], kl[u]));
+          if ((tab.dbnz >> l) & 1u) ev = dadd(ev, dmul(tab.db[l], kl[u]));
+        }
+      }
+      out = dadd(x0e, dmul(xv, E.dt));
+      const double er = dmul(ev, E.dt);
+      E.xnew[idx] = out;
+      const double at = E.atol ? E.atol[idx] : E.atol_s;
+      const double rt = E.rtol ? E.rtol[idx] : E.rtol_s;
+      const double ax = fabs(out), ax0 = fabs(x0e);
+      const double tg = dadd(at, dmul(rt, ax < ax0 ? ax0 : ax));
+      const double q = __ddiv_rn(er, tg);
+      const double sq = dmul(q, q);
+      if (E.exact) {
+        E.sq[idx] = sq;
+      } else {
+        sq_acc = dadd(sq_acc, sq);
+      }
+    }
+    if (pos) part[b_lo + w / 3][w % 3] = out;
+  }
+  if constexpr (PREC == GB_PREC_MIXED) {
+    __syncthreads();
+    PackedBody* dst = E.pnext;
+#pragma unroll 1
+    for (int r = threadIdx.x; r < cnt; r += T) {
+      const double* p = part[b_lo + r];
+      const long long i = i0 + b_lo + r;
+      const float w = E.masses ? (float)E.masses[i] : 1.0f;
+      dst[i] = pack_body(p[0], p[1], p[2], E.cref[0], E.cref[1], E.cref[2], w);
+    }
+  }
+}
+
 // Packs one sorted tile whose bodies' new positions are held one per thread
 // (threadIdx.x < cnt): FP64 centroid and radius by block reductions, then the
 // near record (hi/lo of x - c), the far record (FP32 x - c_J, weight) and the

@@ -115,9 +115,17 @@ __global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 5 * 128 / T)
   E.sq = P.sq;
   double sq_acc = 0.0;
   double amax = 0.0;
+  if constexpr (L >= 2) {
+    // small systems (lanes split each body's partners): the epilogue is a
+    // large share of the launch, one state element per thread
+    rows_epilogue<PREC, T>(E, i0, b_lo, b_hi, part, sq_acc, amax);
+  } else {
+    // one lane per body: one body per thread (measured: the per-element form
+    // slows the pair loop of these instantiations by 12-15 %)
 #pragma unroll 1
-  for (int b = b_lo + (int)threadIdx.x; b < b_hi; b += T)
-    body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
+    for (int b = b_lo + (int)threadIdx.x; b < b_hi; b += T)
+      body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
+  }
   if (last) {
     const double m = block_max(amax, red);
     if (threadIdx.x == 0) P.aux[ci.itile * ci.size + ci.rank] = m;

@@ -103,6 +103,41 @@ def test_fsal_is_bit_identical(gb, torch_cuda):
     assert a[2]["n_rhs_saved"] > 0
 
 
+@pytest.mark.parametrize("n,zero_mass", [(2, False), (3, False), (300, True)])
+def test_element_epilogue_is_bit_identical(gb, torch_cuda, n, zero_mass):
+    """Kernels with two or more lanes per body finish a stage one state
+    element per thread; one-lane kernels one body per thread.  Both do every
+    element's FP64 arithmetic in the same order, so in exact mode (serial
+    error norm), with pair sums that no partner order can change -- at most
+    two partners per body, or zero masses -- one- and two-lane runs, with or
+    without a cluster split, agree bit for bit.  N = 300 puts more elements
+    in a CTA than it has threads."""
+    rng = np.random.default_rng(17 + n)
+    x0 = np.concatenate([rng.uniform(-1, 1, 3 * n), rng.uniform(-0.3, 0.3, 3 * n)])
+    if zero_mass:
+        ode = gb.NBodyODE(n, 0.05, masses=gb.to_device(np.zeros(n)))
+    else:
+        ode = gb.NBodyODE(n, 0.05, 1.0 / n)
+    tab, tol, tf = "RKF78", 1e-10, 0.5
+    runs = {}
+    for split, lanes in [(1, 1), (1, 2), (4, 1), (4, 2)]:
+        exe = gb.Gb300Executor(precision="f64", exact=True, tile=gb.tiling(split, lanes, 0))
+        it = gb.Integrator(tab, ode, exe)
+        it.start(x0, 0.0, tf, tol, tol)
+        geo = it.geometry()
+        it.close()
+        assert (geo["j_split"], geo["lanes"]) == (split, lanes)
+        out = gb.RawOutput()
+        st = gb.RKEmbeddedParallel(tab).integrate(x0, 0.0, tf, tol, tol, ode, out, exe)
+        runs[(split, lanes)] = (np.array(out.times()), np.array(out.states()), st["n_accepted"])
+    t0, s0, a0 = runs[(1, 1)]
+    assert a0 >= 2
+    for key, (t, s, a) in runs.items():
+        assert a == a0, key
+        np.testing.assert_array_equal(t, t0, err_msg=str(key))
+        np.testing.assert_array_equal(s, s0, err_msg=str(key))
+
+
 def test_vector_tolerances_match_scalar(gb, torch_cuda):
     n = 64
     x0 = gb.ic_plummer(n, 3)
