@@ -58,7 +58,7 @@ FLOPS_PER_INTERACTION = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) conven
 HILO_FP32_OPS = 11.5
 # DRAM bytes (read + write) of one headline stage launch from an ncu capture
 # of the same kernel and geometry (python bench.py --workload stage).
-STAGE_DRAM_BYTES_16384 = 2551296
+STAGE_DRAM_BYTES_16384 = 2541312
 FP64_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (non-tensor), one FMA = 2 FLOP
 
 
@@ -137,6 +137,15 @@ def drift(e0: dict, e1: dict) -> dict:
     return {"energy_rel_err": abs(e1["e"] - e0["e"]) / abs(e0["e"]),
             "momentum_drift": float(np.linalg.norm(e1["p"] - e0["p"])),
             "angular_momentum_drift": float(np.linalg.norm(e1["l"] - e0["l"]))}
+
+
+def stage_kernel_name(precision: str, geo: dict) -> str:
+    """The integrator's stage kernel for a geometry: one-lane packed mixed
+    stages run as independent partner chunks, everything else as clusters."""
+    if precision == "mixed" and geo["lanes"] == 1 and geo["j_split"] > 1 \
+            and geo["mixed_variant"] != 1:
+        return f"fused_split_kernel (mixed, one stage, {geo['j_split']} partner chunks per tile)"
+    return f"fused_stage_kernel ({precision}, one stage)"
 
 
 def c1_cpu_baseline(x0: np.ndarray, n: int, eps: float, tol: float) -> dict:
@@ -419,7 +428,7 @@ def main():
                      "traffic_note": "DRAM bytes per launch from one ncu capture of this "
                                      "kernel (compute-bound: positions + stage rows mostly "
                                      "served from L2)",
-                     "kernel": "fused_stage_kernel (mixed, one stage)",
+                     "kernel": stage_kernel_name(W["precision"], geo),
                      "kernel_ms": k_ms, "geometry": geo,
                      "peak_note": f"nominal FP32 pipe: {n_sm} SMs x {FP32_LANES_PER_SM} lanes x 2"
                                   f" x {sm_mhz_max:.0f} MHz ({pk_kind} peaks file has no FP32)",

@@ -135,6 +135,111 @@ __global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 5 * 128 / T)
   if (threadIdx.x == 0) P.partials[ci.itile * ci.size + ci.rank] = tile_sum;
 }
 
+// The packed mixed stage as independent (i-tile, partner chunk) CTAs, without
+// clusters.  Cluster-bound CTAs of one launch drain each SM from seven resident
+// CTAs to one, because the warp schedulers favour older CTAs (measured at
+// N = 16384: identical CTAs finished their pair loops between 45 and 128 us),
+// and an 8-CTA cluster waits for its slowest rank; independent CTAs let the
+// block scheduler refill every SM until the last chunks.  Each CTA stores its
+// FP64 chunk sums; the CTA whose arrival completes the tile's count (an atomic
+// increment, nothing waits) adds the chunks in chunk order, so the sums do not
+// depend on which CTA arrives last, resets the count for the next launch and
+// finishes the tile.
+template <int T, int L, int BPT>
+__global__ void __launch_bounds__(T, 7 * 128 / T)
+    fused_split_kernel(const __grid_constant__ DevTableau tab,
+                       const __grid_constant__ FusedParams P, int s) {
+  constexpr int BI = (T / L) * BPT;
+  constexpr int BW = BI * 3;  // doubles of one chunk's sums
+  __shared__ __align__(16) unsigned char sh_raw[jp_smem_bytes<T>()];
+  __shared__ double part[BI][3];
+  __shared__ double red[T];
+  __shared__ int sh_last;
+  Ctrl* C = P.ctrl;
+  if (C->done) return;
+  const int nc = P.n_chunks;
+  const long long itile = blockIdx.x / nc;
+  const int chunk = (int)(blockIdx.x % nc);
+  const long long n = P.n, n_var = P.n_var;
+  const long long i0 = itile * BI;
+  const bool skip_force = (s == 0 && C->k0_valid);
+  if (skip_force) {
+    if (chunk != 0) return;  // the stage derivative is reused: one CTA per tile
+  } else {
+    long long jb, je;
+    j_chunk(n, chunk, nc, 2, jb, je);
+    const PackedBody* src =
+        (s == 0) ? P.PX + (long long)C->px * n : P.PY + (long long)(s & 1) * n;
+    force_mixed_cta_jp<T, L, BPT>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
+    __syncthreads();
+    const double* pf = &part[0][0];
+    double* mine = P.chunk_sums + (long long)blockIdx.x * BW;
+    for (int e = threadIdx.x; e < BW; e += T) mine[e] = pf[e];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) sh_last = atomicAdd(P.tile_count + itile, 1u) == (unsigned)(nc - 1);
+    __syncthreads();
+    if (!sh_last) return;
+    __threadfence();
+    const double* g0 = P.chunk_sums + itile * nc * BW;
+    double* pw = &part[0][0];
+    for (int e = threadIdx.x; e < BW; e += T) {
+      double v = __ldcg(g0 + e);
+      for (int c = 1; c < nc; ++c) v = dadd(v, __ldcg(g0 + (long long)c * BW + e));
+      pw[e] = v;
+    }
+    if (threadIdx.x == 0) P.tile_count[itile] = 0u;
+    __syncthreads();
+  }
+  const int cur = C->cur;
+  const int px = C->px;
+  const int S = tab.n_stages;
+  const bool last = (s == S - 1);
+  const double* x0 = P.ring + (long long)cur * n_var;
+  EpiCtx E;
+  E.tab = &tab;
+  E.s = s;
+  E.S = S;
+  E.k0slot = C->k0slot;
+  E.skip_force = skip_force;
+  E.last = last;
+  E.exact = P.exact != 0;
+  E.dt = C->dt;
+  E.n = n;
+  E.x0 = x0;
+  E.ysrc = (s == 0) ? x0 : P.Y + (long long)(s & 1) * n_var;
+  E.ks = P.ks;
+  E.kstride = n_var;
+  E.ynext = P.Y + (long long)((s + 1) & 1) * n_var;
+  E.xnew = P.ring + (long long)((cur + 1) % P.R) * n_var;
+  E.pnext = last ? P.PX + (long long)(px ^ 1) * n : P.PY + (long long)((s + 1) & 1) * n;
+  E.atol = P.atol;
+  E.rtol = P.rtol;
+  E.atol_s = P.atol_s;
+  E.rtol_s = P.rtol_s;
+  E.masses = P.masses;
+  E.mass = P.mass;
+  E.cref = P.cref;
+  E.sq = P.sq;
+  const int b_hi = (int)min((long long)BI, n - i0);
+  double sq_acc = 0.0;
+  double amax = 0.0;
+  if constexpr (L >= 2) {
+    rows_epilogue<GB_PREC_MIXED, T>(E, i0, 0, b_hi, part, sq_acc, amax);
+  } else {
+#pragma unroll 1
+    for (int b = threadIdx.x; b < b_hi; b += T)
+      body_epilogue<GB_PREC_MIXED>(E, i0 + b, part[b], sq_acc, amax);
+  }
+  if (last) {
+    const double m = block_max(amax, red);
+    if (threadIdx.x == 0) P.aux[itile] = m;
+  }
+  if (!last) return;
+  const double tile_sum = block_sum(sq_acc, red);
+  if (threadIdx.x == 0) P.partials[itile] = tile_sum;
+}
+
 // The mixed-precision stage on Morton-sorted tiles: i-tile = 128 consecutive
 // sorted bodies, far j-tiles through the tile-centroid records, the epilogue
 // repacks the CTA's own tile (centroid, radius, near and far records) for
@@ -498,6 +603,16 @@ const void* pick_packed(int L) {
   }
 }
 
+template <int BPT>
+const void* pick_split(int L) {
+  switch (L) {
+    case 1: return (const void*)fused_split_kernel<128, 1, BPT>;
+    case 2: return (const void*)fused_split_kernel<128, 2, BPT>;
+    case 4: return (const void*)fused_split_kernel<128, 4, BPT>;
+    default: return nullptr;
+  }
+}
+
 const void* pick_fused(int prec, int T, int L, int BPT, bool packed = false) {
   if (prec == GB_PREC_MIXED && packed) {
     if (T == 128 && BPT == 1) return pick_packed<128, 1>(L);
@@ -558,6 +673,8 @@ struct gb_integrator_s {
   gb_integrate_opts opts;
   gb::ForceGeom geom;
   const void* kernel = nullptr;
+  bool split = false;               // packed mixed stage as independent partner chunks
+  gb_force_tiling start_tiling{};   // right-hand sides of the initial step
   cudaStream_t user_stream = nullptr;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -602,6 +719,8 @@ struct gb_integrator_s {
   double* dense_out = nullptr;
   long long n_dense = 0;
   void* mlp_dev = nullptr;
+  double* chunk_sums = nullptr;
+  unsigned* tile_count = nullptr;
   // host
   gb::Ctrl* hctrl = nullptr;  // pinned
   double* hstage = nullptr;   // pinned R * n_var (recording)
@@ -639,7 +758,8 @@ void free_all(gb_integrator_s* it) {
                   it->PY,    it->atol, it->rtol,       it->cref,   it->partials, it->aux,
                   it->sq,    it->dscal, it->norm_work, it->masses, it->log,      it->mlp_dev,
                   it->perm,  it->vals, it->keys,     it->keys_alt, it->cub_temp, it->bbox,
-                  it->PXF,   it->PYF,  it->MX,       it->MY,       it->dense_t, it->dense_out};
+                  it->PXF,   it->PYF,  it->MX,       it->MY,       it->dense_t, it->dense_out,
+                  it->chunk_sums, it->tile_count};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (it->hctrl) cudaFreeHost(it->hctrl);
@@ -649,9 +769,16 @@ void free_all(gb_integrator_s* it) {
   if (it->stream && it->own_stream) cudaStreamDestroy(it->stream);
 }
 
+int launch_stage_kernel(gb_integrator_s* it, void** args) {
+  if (!it->split) return launch_cluster(it->kernel, it->geom, 0, it->stream, args);
+  const dim3 grid((unsigned)(it->geom.n_itiles * it->geom.P)), block((unsigned)it->geom.T);
+  GB_CUDA_TRY(cudaLaunchKernel(it->kernel, grid, block, args, 0, it->stream));
+  return GB_OK;
+}
+
 int launch_fused(gb_integrator_s* it, int s) {
   void* args[] = {(void*)&it->tab, (void*)&it->params, (void*)&s};
-  GB_TRY(launch_cluster(it->kernel, it->geom, 0, it->stream, args));
+  GB_TRY(launch_stage_kernel(it, args));
   if (s == it->S - 1) {
     control_kernel<<<1, 256, 0, it->stream>>>(it->tab, it->params);
     GB_CUDA_TRY(cudaGetLastError());
@@ -781,10 +908,30 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
     if (it->geom.L > 2) it->geom.L = 2;
     it->geom.BPT = it->geom.L;  // i-tile = j-tile = T bodies
   }
+  // One-lane packed mixed stages run as independent partner chunks
+  // (fused_split_kernel); from N = 8192 one lane per body with chunks of about
+  // 1024 partners, at most 32 per tile (measured per RKF78 stage: N = 8192
+  // 0.0563 ms against 0.0594 ms for clusters of 8 x 2 lanes; 16384 0.142
+  // against 0.155; 32768 0.470 against 0.513; 131072 6.88 against 7.37).
+  if (!it->sorted && opts.precision == GB_PREC_MIXED && it->geom.variant != 1 && !opts.exact) {
+    if (it->n >= 8192) {
+      if (opts.tiling.lanes <= 0) it->geom.L = 1;
+      if (it->geom.L == 1 && opts.tiling.j_split <= 0) {
+        int P = 8;
+        while (P < 32 && (long long)P * 2 * 1024 <= it->n) P *= 2;
+        it->geom.P = P;
+      }
+    }
+    it->split = it->geom.L == 1 && it->geom.P > 1;
+  }
   it->geom.n_itiles = (it->n + it->geom.bodies_per_cta() - 1) / it->geom.bodies_per_cta();
   it->kernel = it->sorted ? pick_sorted(it->geom.T, it->geom.L, sys->masses_dev == nullptr)
                           : pick_fused(opts.precision, it->geom.T, it->geom.L, it->geom.BPT,
                                        it->geom.variant != 1);
+  if (it->split)
+    it->kernel = it->geom.BPT == 1 ? pick_split<1>(it->geom.L) : pick_split<2>(it->geom.L);
+  it->start_tiling = opts.tiling;
+  if (it->start_tiling.j_split > 8) it->start_tiling.j_split = 8;
   int rc = GB_OK;
   auto fail = [&](int code) {
     free_all(it);
@@ -792,7 +939,7 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
     return code;
   };
   if (!it->kernel) return fail(GB_ERR_UNSUPPORTED);
-  if (it->geom.P > 8 &&
+  if (!it->split && it->geom.P > 8 &&
       cudaFuncSetAttribute(it->kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
           cudaSuccess)
     return fail(GB_ERR_UNSUPPORTED);  // 16-CTA clusters opt-in before any graph capture
@@ -818,6 +965,11 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   GB_ALLOC(it->aux, n_parts * sizeof(double));
   e = cudaMemset(it->partials, 0, n_parts * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(it->aux, 0, n_parts * sizeof(double));
+  if (e == cudaSuccess && it->split) {
+    GB_ALLOC(it->chunk_sums, n_parts * 3 * (size_t)it->geom.bodies_per_cta() * sizeof(double));
+    GB_ALLOC(it->tile_count, (size_t)it->geom.n_itiles * sizeof(unsigned));
+    e = cudaMemset(it->tile_count, 0, (size_t)it->geom.n_itiles * sizeof(unsigned));
+  }
   if (e != cudaSuccess) {
     note_cuda_error(e);
     return fail(GB_ERR_CUDA);
@@ -907,7 +1059,10 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   P.n = n;
   P.n_var = nv;
   P.n_itiles = it->geom.n_itiles;
-  P.n_parts = it->geom.n_itiles * it->geom.P;
+  P.n_parts = it->split ? it->geom.n_itiles : it->geom.n_itiles * it->geom.P;
+  P.n_chunks = it->split ? it->geom.P : 1;
+  P.chunk_sums = it->chunk_sums;
+  P.tile_count = it->tile_count;
   P.exact = opts.exact;
   P.S = it->S;
   P.perm = it->perm;
@@ -965,7 +1120,7 @@ extern "C" int gb_integrator_start(gb_integrator it, const double* x0, double t0
   GB_CUDA_TRY(cudaGetLastError());
   const gb_nbody_system& sys = it->sys;
   GB_TRY(rhs_for_start(prec, it->ring, f0, n, sys.softening, sys.mass, it->masses, it->PX,
-                       it->opts.exact, &it->opts.tiling, s));
+                       it->opts.exact, &it->start_tiling, s));
   double* d = it->dscal;
   if (it->opts.exact) {
     serial_norm_kernel<<<1, 32, 0, s>>>(it->ring, tg, nv, d + 0);
@@ -982,7 +1137,7 @@ extern "C" int gb_integrator_start(gb_integrator it, const double* x0, double t0
     GB_CUDA_TRY(cudaGetLastError());
   }
   GB_TRY(rhs_for_start(prec, x1, df, n, sys.softening, sys.mass, it->masses, it->PY,
-                       it->opts.exact, &it->opts.tiling, s));
+                       it->opts.exact, &it->start_tiling, s));
   diff_kernel<<<blocks256(nv), 256, 0, s>>>(df, f0, nv);
   GB_CUDA_TRY(cudaGetLastError());
   if (it->opts.exact) {
@@ -1096,7 +1251,7 @@ extern "C" int gb_integrator_dense_output(gb_integrator it, double* x_host, int6
 extern "C" int gb_integrator_launch_stage(gb_integrator it, int32_t stage) {
   if (!it || !it->started || stage < 0 || stage >= it->S) return GB_ERR_INVALID_ARGUMENT;
   void* args[] = {(void*)&it->tab, (void*)&it->params, (void*)&stage};
-  return launch_cluster(it->kernel, it->geom, 0, it->stream, args);
+  return launch_stage_kernel(it, args);
 }
 
 extern "C" int gb_integrator_geometry(gb_integrator it, gb_force_tiling* out, int64_t* n_ctas) {

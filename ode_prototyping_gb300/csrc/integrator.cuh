@@ -80,6 +80,10 @@ struct FusedParams {
   long long n, n_var, n_itiles, n_parts;
   int exact;
   int S;
+  // partner-chunk split without clusters (packed mixed path)
+  int n_chunks;          // partner chunks per i-tile
+  double* chunk_sums;    // n_itiles * n_chunks * 3 * bodies per tile
+  unsigned* tile_count;  // n_itiles arrival counts, zero between launches
   // spatially sorted mixed path
   const int* perm;       // sorted position -> body
   float4* PXF;           // 2 * n far records (x0 / x_new)

@@ -138,6 +138,46 @@ def test_element_epilogue_is_bit_identical(gb, torch_cuda, n, zero_mass):
         np.testing.assert_array_equal(s, s0, err_msg=str(key))
 
 
+def _mixed_run(gb, ode, x0, tf, tol, tile=None, variant=0):
+    exe = gb.Gb300Executor(precision="mixed", tile=tile if tile is not None
+                           else gb.tiling(mixed_variant=variant))
+    out = gb.RawOutput()
+    st = gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, tf, tol, tol, ode, out, exe)
+    return np.array(out.times()), np.array(out.states()), st
+
+
+def test_split_stage_is_deterministic_and_tracks_fp64(gb, torch_cuda):
+    """From N = 8192 the packed mixed stage runs as independent partner chunks
+    whose sums the last-arriving CTA adds in chunk order.  Runs are bit for
+    bit repeatable whatever the arrival order; the chunked form, the cluster
+    form (8 x 2 lanes), an uneven chunk count (5) and the two-bodies-per-thread
+    loop all follow the FP64 integration to the mixed-precision bound."""
+    n, soft, tol, tf = 8192, 0.01, 1e-9, 0.02
+    x0 = gb.ic_plummer(n, 77)
+    ode = gb.NBodyODE(n, soft, 1.0 / n)
+    exe = gb.Gb300Executor(precision="mixed")
+    it = gb.Integrator("DOPRI5", ode, exe)
+    it.start(x0, 0.0, tf, tol, tol)
+    geo = it.geometry()
+    it.close()
+    assert (geo["j_split"], geo["lanes"]) == (8, 1)
+    a = _mixed_run(gb, ode, x0, tf, tol)
+    b = _mixed_run(gb, ode, x0, tf, tol)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    out64 = gb.RawOutput()
+    gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, tf, tol, tol, ode, out64,
+                                              gb.Gb300Executor(precision="f64"))
+    ref = np.array(out64.states()[-1])
+    runs = {"split": a, "cluster": _mixed_run(gb, ode, x0, tf, tol, tile=gb.tiling(8, 2, 0)),
+            "split5": _mixed_run(gb, ode, x0, tf, tol, tile=gb.tiling(5, 1, 0)),
+            "pairs2": _mixed_run(gb, ode, x0, tf, tol, variant=2)}
+    for name, (t, s, st) in runs.items():
+        assert t[-1] == tf, name
+        assert abs(len(t) - len(out64.times())) <= 2, name
+        assert np.max(np.abs(s[-1] - ref)) <= 1e-6, name
+
+
 def test_vector_tolerances_match_scalar(gb, torch_cuda):
     n = 64
     x0 = gb.ic_plummer(n, 3)
