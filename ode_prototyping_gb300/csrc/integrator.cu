@@ -157,23 +157,24 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
   __shared__ int sh_last;
   Ctrl* C = P.ctrl;
   if (C->done) return;
+  // chunk-major order: every tile's chunk 0, then every tile's chunk 1, ...;
+  // the schedule puts the larger chunks first, so the last CTAs are short
   const int nc = P.n_chunks;
-  const long long itile = blockIdx.x / nc;
-  const int chunk = (int)(blockIdx.x % nc);
+  const long long itile = blockIdx.x % P.n_itiles;
+  const int chunk = (int)(blockIdx.x / P.n_itiles);
   const long long n = P.n, n_var = P.n_var;
   const long long i0 = itile * BI;
   const bool skip_force = (s == 0 && C->k0_valid);
   if (skip_force) {
     if (chunk != 0) return;  // the stage derivative is reused: one CTA per tile
   } else {
-    long long jb, je;
-    j_chunk(n, chunk, nc, 2, jb, je);
+    const long long jb = P.chunk_start[chunk], je = P.chunk_start[chunk + 1];
     const PackedBody* src =
         (s == 0) ? P.PX + (long long)C->px * n : P.PY + (long long)(s & 1) * n;
     force_mixed_cta_jp<T, L, BPT>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
     __syncthreads();
     const double* pf = &part[0][0];
-    double* mine = P.chunk_sums + (long long)blockIdx.x * BW;
+    double* mine = P.chunk_sums + (itile * nc + chunk) * BW;
     for (int e = threadIdx.x; e < BW; e += T) mine[e] = pf[e];
     __threadfence();
     __syncthreads();
@@ -674,6 +675,7 @@ struct gb_integrator_s {
   gb::ForceGeom geom;
   const void* kernel = nullptr;
   bool split = false;               // packed mixed stage as independent partner chunks
+  std::vector<long long> chunks;    // partner chunk boundaries of the split stage
   gb_force_tiling start_tiling{};   // right-hand sides of the initial step
   cudaStream_t user_stream = nullptr;
   cudaStream_t stream = nullptr;
@@ -767,6 +769,16 @@ void free_all(gb_integrator_s* it) {
   if (it->htimes) cudaFreeHost(it->htimes);
   if (it->ev) cudaEventDestroy(it->ev);
   if (it->stream && it->own_stream) cudaStreamDestroy(it->stream);
+}
+
+// Partner chunk boundaries of the split stage kernel: nc chunks of equal
+// length in partner pairs (the packed loop takes any run of pairs).
+std::vector<long long> split_schedule(long long n, int nc) {
+  const long long pairs = (n + 1) / 2, per = (pairs + nc - 1) / nc;
+  std::vector<long long> b;
+  for (int c = 0; c < nc; ++c) b.push_back(std::min(n, 2 * per * c));
+  b.push_back(n);
+  return b;
 }
 
 int launch_stage_kernel(gb_integrator_s* it, void** args) {
@@ -923,6 +935,10 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
       }
     }
     it->split = it->geom.L == 1 && it->geom.P > 1;
+    if (it->split) {
+      it->chunks = split_schedule(it->n, std::min(it->geom.P, kMaxChunks));
+      it->geom.P = (int)it->chunks.size() - 1;
+    }
   }
   it->geom.n_itiles = (it->n + it->geom.bodies_per_cta() - 1) / it->geom.bodies_per_cta();
   it->kernel = it->sorted ? pick_sorted(it->geom.T, it->geom.L, sys->masses_dev == nullptr)
@@ -1061,6 +1077,8 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   P.n_itiles = it->geom.n_itiles;
   P.n_parts = it->split ? it->geom.n_itiles : it->geom.n_itiles * it->geom.P;
   P.n_chunks = it->split ? it->geom.P : 1;
+  for (int c = 0; c <= kMaxChunks; ++c)
+    P.chunk_start[c] = c < (int)it->chunks.size() ? it->chunks[c] : n;
   P.chunk_sums = it->chunk_sums;
   P.tile_count = it->tile_count;
   P.exact = opts.exact;

@@ -54,6 +54,9 @@ struct StepLog {
   float log_dt_ideal; // log of the step the I-controller formula proposes
 };
 
+// most partner chunks per i-tile in the split stage kernel
+constexpr int kMaxChunks = 32;
+
 struct FusedParams {
   Ctrl* ctrl;
   double* ring;        // R * n_var states; x0 = ring + cur * n_var
@@ -84,6 +87,7 @@ struct FusedParams {
   int n_chunks;          // partner chunks per i-tile
   double* chunk_sums;    // n_itiles * n_chunks * 3 * bodies per tile
   unsigned* tile_count;  // n_itiles arrival counts, zero between launches
+  long long chunk_start[kMaxChunks + 1];  // partner range of chunk c: [start[c], start[c+1])
   // spatially sorted mixed path
   const int* perm;       // sorted position -> body
   float4* PXF;           // 2 * n far records (x0 / x_new)
