@@ -196,6 +196,23 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
+// Knuth's error-free sum: s + e == a + b exactly (explicit IEEE adds, so
+// nothing is contracted or reassociated).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (S, E) += (hi, lo) in double-single arithmetic (an unevaluated sum of two
+// floats, about 48 significant bits), renormalised after each addition.
+__device__ __forceinline__ void ds_add(float& S, float& E, float hi, float lo) {
+  float s, e;
+  two_sum(S, hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(E, lo));
+  two_sum(s, e, S, E);
+}
+
 // Pair differences.  With hi = fl32(x - c) and lo = fl32(x - c - hi) (c the
 // reference point), the hi-only difference hj - hi is off by at most
 // 2^-24 (|x_i - c| + |x_j - c|) + 2^-24 |dx|, i.e. relatively by
@@ -403,7 +420,9 @@ constexpr int jp_smem_bytes() {
   return 2 * (int)sizeof(PartnerPair) * T + 2 * T * (int)sizeof(PackedBody);
 }
 
-template <int T, int L, int NB = 1>
+// PAIRS (one lane per body): part is read as float2[BI][3] and receives each
+// sum as its FP32 Kahan pair (s, -c), value s - c, with no FP64 arithmetic.
+template <int T, int L, int NB = 1, bool PAIRS = false>
 __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict__ packed,
                                                    long long n, long long i0, long long jb,
                                                    long long je, float eps2, unsigned char* smem,
@@ -574,18 +593,29 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     }
     __syncthreads();
   }
+  if constexpr (PAIRS) {
+    static_assert(L == 1, "Kahan pairs out: one lane per body");
+    float2(*pf)[3] = reinterpret_cast<float2(*)[3]>(part);
 #pragma unroll
-  for (int q = 0; q < NB; ++q) {
-    double ax = dsub((double)sx[q], (double)cx[q]);
-    double ay = dsub((double)sy[q], (double)cy[q]);
-    double az = dsub((double)sz[q], (double)cz[q]);
-    ax = lane_reduce<L>(ax);
-    ay = lane_reduce<L>(ay);
-    az = lane_reduce<L>(az);
-    if (l == 0) {
-      part[q * BG + g][0] = ax;
-      part[q * BG + g][1] = ay;
-      part[q * BG + g][2] = az;
+    for (int q = 0; q < NB; ++q) {
+      pf[q * BG + g][0] = make_float2(sx[q], -cx[q]);
+      pf[q * BG + g][1] = make_float2(sy[q], -cy[q]);
+      pf[q * BG + g][2] = make_float2(sz[q], -cz[q]);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      double ax = dsub((double)sx[q], (double)cx[q]);
+      double ay = dsub((double)sy[q], (double)cy[q]);
+      double az = dsub((double)sz[q], (double)cz[q]);
+      ax = lane_reduce<L>(ax);
+      ay = lane_reduce<L>(ay);
+      az = lane_reduce<L>(az);
+      if (l == 0) {
+        part[q * BG + g][0] = ax;
+        part[q * BG + g][1] = ay;
+        part[q * BG + g][2] = az;
+      }
     }
   }
 }

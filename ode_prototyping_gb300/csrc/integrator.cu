@@ -171,10 +171,11 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
     const long long jb = P.chunk_start[chunk], je = P.chunk_start[chunk + 1];
     const PackedBody* src =
         (s == 0) ? P.PX + (long long)C->px * n : P.PY + (long long)(s & 1) * n;
-    force_mixed_cta_jp<T, L, BPT>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
+    force_mixed_cta_jp<T, L, BPT, true>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
     __syncthreads();
-    const double* pf = &part[0][0];
-    double* mine = P.chunk_sums + (itile * nc + chunk) * BW;
+    // the chunk's sums leave as FP32 Kahan pairs (s, -c)
+    const float2* pf = reinterpret_cast<const float2*>(&part[0][0]);
+    float2* mine = reinterpret_cast<float2*>(P.chunk_sums) + (itile * nc + chunk) * BW;
     for (int e = threadIdx.x; e < BW; e += T) mine[e] = pf[e];
     __threadfence();
     __syncthreads();
@@ -182,12 +183,17 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
     __syncthreads();
     if (!sh_last) return;
     __threadfence();
-    const double* g0 = P.chunk_sums + itile * nc * BW;
+    // chunks added in chunk order in double-single FP32 arithmetic (the FP64
+    // pipe runs at 1/64 of the FP32 rate), one conversion per component
+    const float2* g0 = reinterpret_cast<const float2*>(P.chunk_sums) + itile * nc * BW;
     double* pw = &part[0][0];
     for (int e = threadIdx.x; e < BW; e += T) {
-      double v = __ldcg(g0 + e);
-      for (int c = 1; c < nc; ++c) v = dadd(v, __ldcg(g0 + (long long)c * BW + e));
-      pw[e] = v;
+      float S = 0.f, E = 0.f;
+      for (int c = 0; c < nc; ++c) {
+        const float2 v = __ldcg(g0 + (long long)c * BW + e);
+        ds_add(S, E, v.x, v.y);
+      }
+      pw[e] = dadd((double)S, (double)E);
     }
     if (threadIdx.x == 0) P.tile_count[itile] = 0u;
     __syncthreads();
@@ -606,12 +612,7 @@ const void* pick_packed(int L) {
 
 template <int BPT>
 const void* pick_split(int L) {
-  switch (L) {
-    case 1: return (const void*)fused_split_kernel<128, 1, BPT>;
-    case 2: return (const void*)fused_split_kernel<128, 2, BPT>;
-    case 4: return (const void*)fused_split_kernel<128, 4, BPT>;
-    default: return nullptr;
-  }
+  return L == 1 ? (const void*)fused_split_kernel<128, 1, BPT> : nullptr;
 }
 
 const void* pick_fused(int prec, int T, int L, int BPT, bool packed = false) {

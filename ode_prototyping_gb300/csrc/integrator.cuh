@@ -85,7 +85,7 @@ struct FusedParams {
   int S;
   // partner-chunk split without clusters (packed mixed path)
   int n_chunks;          // partner chunks per i-tile
-  double* chunk_sums;    // n_itiles * n_chunks * 3 * bodies per tile
+  double* chunk_sums;    // n_itiles * n_chunks * 3 * bodies per tile, 8 bytes each
   unsigned* tile_count;  // n_itiles arrival counts, zero between launches
   long long chunk_start[kMaxChunks + 1];  // partner range of chunk c: [start[c], start[c+1])
   // spatially sorted mixed path
