@@ -58,7 +58,7 @@ FLOPS_PER_INTERACTION = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) conven
 HILO_FP32_OPS = 11.5
 # DRAM bytes (read + write) of one headline stage launch from an ncu capture
 # of the same kernel and geometry (python bench.py --workload stage).
-STAGE_DRAM_BYTES_16384 = 2541312
+STAGE_DRAM_BYTES_16384 = 2542592
 FP64_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (non-tensor), one FMA = 2 FLOP
 
 
