@@ -104,7 +104,10 @@ int gb_pointer_kind(const void* ptr);
 /* ---------------------------------------------------------------------- */
 typedef struct {
   int32_t j_split;       /* CTAs per thread-block cluster sharing one i-tile: 1,2,4,8,16
-                            (0 = auto; 16 is a non-portable cluster size) */
+                            (0 = auto; 16 is a non-portable cluster size).  The
+                            integrator's mixed stage with one lane per body (packed
+                            loops, from N = 8192 by default) reads it as independent
+                            partner chunks per i-tile, no clusters: 2..32 */
   int32_t lanes;         /* lanes per body inside a warp: 1,2,4,8 (0 = auto) */
   int32_t bodies_per_cta;/* i-bodies per CTA: 32..256 (0 = auto) */
   int32_t mixed_variant; /* mixed-precision pair loop: 0 = auto (3), 1 = scalar FP32 (two

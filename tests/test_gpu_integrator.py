@@ -146,13 +146,15 @@ def _mixed_run(gb, ode, x0, tf, tol, tile=None, variant=0):
     return np.array(out.times()), np.array(out.states()), st
 
 
-def test_split_stage_is_deterministic_and_tracks_fp64(gb, torch_cuda):
+@pytest.mark.parametrize("n", [8192, 8333])
+def test_split_stage_is_deterministic_and_tracks_fp64(gb, torch_cuda, n):
     """From N = 8192 the packed mixed stage runs as independent partner chunks
     whose sums the last-arriving CTA adds in chunk order.  Runs are bit for
     bit repeatable whatever the arrival order; the chunked form, the cluster
     form (8 x 2 lanes), an uneven chunk count (5) and the two-bodies-per-thread
-    loop all follow the FP64 integration to the mixed-precision bound."""
-    n, soft, tol, tf = 8192, 0.01, 1e-9, 0.02
+    loop all follow the FP64 integration to the mixed-precision bound.
+    N = 8333 leaves a ragged last tile and an odd partner count."""
+    soft, tol, tf = 0.01, 1e-9, 0.02
     x0 = gb.ic_plummer(n, 77)
     ode = gb.NBodyODE(n, soft, 1.0 / n)
     exe = gb.Gb300Executor(precision="mixed")
