@@ -141,10 +141,10 @@ __global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 5 * 128 / T)
 // N = 16384: identical CTAs finished their pair loops between 45 and 128 us),
 // and an 8-CTA cluster waits for its slowest rank; independent CTAs let the
 // block scheduler refill every SM until the last chunks.  Each CTA stores its
-// FP64 chunk sums; the CTA whose arrival completes the tile's count (an atomic
-// increment, nothing waits) adds the chunks in chunk order, so the sums do not
-// depend on which CTA arrives last, resets the count for the next launch and
-// finishes the tile.
+// chunk's sums as FP32 Kahan pairs; the CTA whose arrival completes the tile's
+// count (an atomic increment, nothing waits) adds the chunks in chunk order,
+// so the sums do not depend on which CTA arrives last, resets the count for
+// the next launch and finishes the tile.
 template <int T, int L, int BPT>
 __global__ void __launch_bounds__(T, 7 * 128 / T)
     fused_split_kernel(const __grid_constant__ DevTableau tab,
@@ -157,8 +157,8 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
   __shared__ int sh_last;
   Ctrl* C = P.ctrl;
   if (C->done) return;
-  // chunk-major order: every tile's chunk 0, then every tile's chunk 1, ...;
-  // the schedule puts the larger chunks first, so the last CTAs are short
+  // chunk-major order: every tile's chunk 0, then every tile's chunk 1, ...
+  // (chunk boundaries from the table in the parameters)
   const int nc = P.n_chunks;
   const long long itile = blockIdx.x % P.n_itiles;
   const int chunk = (int)(blockIdx.x / P.n_itiles);
