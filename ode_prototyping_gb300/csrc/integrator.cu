@@ -149,6 +149,7 @@ template <int T, int L, int BPT>
 __global__ void __launch_bounds__(T, 7 * 128 / T)
     fused_split_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ FusedParams P, int s) {
+  static_assert(L == 1, "partner chunks: one lane per body");
   constexpr int BI = (T / L) * BPT;
   constexpr int BW = BI * 3;  // doubles of one chunk's sums
   __shared__ __align__(16) unsigned char sh_raw[jp_smem_bytes<T>()];
@@ -231,13 +232,9 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
   const int b_hi = (int)min((long long)BI, n - i0);
   double sq_acc = 0.0;
   double amax = 0.0;
-  if constexpr (L >= 2) {
-    rows_epilogue<GB_PREC_MIXED, T>(E, i0, 0, b_hi, part, sq_acc, amax);
-  } else {
 #pragma unroll 1
-    for (int b = threadIdx.x; b < b_hi; b += T)
-      body_epilogue<GB_PREC_MIXED>(E, i0 + b, part[b], sq_acc, amax);
-  }
+  for (int b = threadIdx.x; b < b_hi; b += T)
+    body_epilogue<GB_PREC_MIXED>(E, i0 + b, part[b], sq_acc, amax);
   if (last) {
     const double m = block_max(amax, red);
     if (threadIdx.x == 0) P.aux[itile] = m;
