@@ -440,6 +440,7 @@ def main():
         line["e2e"] = e2e(gb, torch, x0)
         if not args.no_fp64:
             line["fp64_comparison"] = fp64_compare(gb, torch, x0, line)
+            line["equal_energy_le_1e-8"] = energy_target_compare(gb, torch, x0)
         if not args.no_cpu_baseline:
             try:
                 line["cpu_baseline"] = cpu_baseline(attempts / max(accepted, 1))
@@ -838,6 +839,55 @@ def fp64_compare(gb, torch, x0, line, k: int = 6) -> dict:
     res["speedup_mixed_vs_f64"] = (res["mixed"]["accepted_steps_per_s"] /
                                    max(res["f64"]["accepted_steps_per_s"], 1e-30))
     return res
+
+
+def energy_target_compare(gb, torch, x0, tol: float = 1e-11, skip: int = 4,
+                          k: int = 8) -> dict:
+    """The same system at a tolerance where the relative energy error over
+    t0 -> tf is at most 1e-8: the mixed path's whole trajectory (its energy
+    error measured) and the plain FP64 path's throughput over k attempts at
+    the same tolerance after `skip` untimed start-up attempts (the FP64 whole
+    trajectory takes minutes: python bench.py --workload c2_tol --tol 1e-11)."""
+    W = WORKLOAD
+    n = W["n_particles"]
+    stream = torch.cuda.Stream()
+    out = {"tol": tol}
+    for prec in ("mixed", "f64"):
+        exe = gb.Gb300Executor(precision=prec, attempts_per_sync=16 if prec == "mixed" else 1)
+        it = gb.Integrator(W["tableau"], gb.NBodyODE(n, W["softening"], 1.0 / n), exe,
+                           stream=stream)
+        it.start(x0, W["t0"], W["tf"], tol, tol)
+        it.sync()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        if prec == "f64":
+            it.enqueue(skip)
+            it.sync()
+        s0 = it.stats()
+        a.record(stream)
+        if prec == "mixed":
+            it.advance(0)
+        else:
+            it.enqueue(k)
+        b.record(stream)
+        stream.synchronize()
+        it.sync()
+        s1 = it.stats()
+        xs, t = it.state()
+        ms = a.elapsed_time(b)
+        r = {"accepted_steps_per_s": (s1["n_accepted"] - s0["n_accepted"]) / (ms / 1e3),
+             "accepted": s1["n_accepted"] - s0["n_accepted"],
+             "attempts": s1["n_attempts"] - s0["n_attempts"], "t_reached": t, "ms": ms}
+        if prec == "mixed":
+            e0 = gb.energy(x0, n, W["softening"], 1.0 / n)
+            r.update(drift(e0, gb.energy(xs, n, W["softening"], 1.0 / n)))
+        else:
+            r["window"] = f"{k} attempts after {skip} start-up attempts"
+        out[prec] = r
+        it.close()
+    out["speedup_mixed_vs_f64"] = (out["mixed"]["accepted_steps_per_s"] /
+                                   max(out["f64"]["accepted_steps_per_s"], 1e-30))
+    return out
 
 
 if __name__ == "__main__":
