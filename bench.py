@@ -844,16 +844,26 @@ def fp64_compare(gb, torch, x0, line, k: int = 6) -> dict:
 def energy_target_compare(gb, torch, x0, tol: float = 1e-11, skip: int = 4,
                           k: int = 8) -> dict:
     """The same system at a tolerance where the relative energy error over
-    t0 -> tf is at most 1e-8: the mixed path's whole trajectory (its energy
-    error measured) and the plain FP64 path's throughput over k attempts at
-    the same tolerance after `skip` untimed start-up attempts (the FP64 whole
-    trajectory takes minutes: python bench.py --workload c2_tol --tol 1e-11)."""
+    t0 -> tf is at most 1e-8: the mixed path's whole trajectory with the
+    reference controller and with the learned proposer trained at this
+    tolerance (energy errors measured), and the plain FP64 path's throughput
+    over k attempts at the same tolerance after `skip` untimed start-up
+    attempts (the FP64 whole trajectory takes minutes: python bench.py
+    --workload c2_tol --tol 1e-11)."""
     W = WORKLOAD
     n = W["n_particles"]
     stream = torch.cuda.Stream()
     out = {"tol": tol}
-    for prec in ("mixed", "f64"):
-        exe = gb.Gb300Executor(precision=prec, attempts_per_sync=16 if prec == "mixed" else 1)
+    # the proposer trained at this tolerance (ode_prototyping_gb300/learned.py)
+    mlp = gb.GbMlp.from_buffer_copy(open(os.path.join(
+        ROOT, "ode_prototyping_gb300", "weights", "proposer_plummer16384_rkf78_tol1e-11.bin"),
+        "rb").read())
+    for key in ("mixed", "mixed_learned", "f64"):
+        prec = "f64" if key == "f64" else "mixed"
+        learned = key == "mixed_learned"
+        exe = gb.Gb300Executor(precision=prec, attempts_per_sync=16 if prec == "mixed" else 1,
+                               controller="learned" if learned else "reference",
+                               mlp=mlp if learned else None)
         it = gb.Integrator(W["tableau"], gb.NBodyODE(n, W["softening"], 1.0 / n), exe,
                            stream=stream)
         it.start(x0, W["t0"], W["tf"], tol, tol)
@@ -877,16 +887,20 @@ def energy_target_compare(gb, torch, x0, tol: float = 1e-11, skip: int = 4,
         ms = a.elapsed_time(b)
         r = {"accepted_steps_per_s": (s1["n_accepted"] - s0["n_accepted"]) / (ms / 1e3),
              "accepted": s1["n_accepted"] - s0["n_accepted"],
-             "attempts": s1["n_attempts"] - s0["n_attempts"], "t_reached": t, "ms": ms}
+             "attempts": s1["n_attempts"] - s0["n_attempts"],
+             "rhs_evals": s1["n_rhs"] - s0["n_rhs"], "t_reached": t, "ms": ms}
         if prec == "mixed":
             e0 = gb.energy(x0, n, W["softening"], 1.0 / n)
             r.update(drift(e0, gb.energy(xs, n, W["softening"], 1.0 / n)))
         else:
             r["window"] = f"{k} attempts after {skip} start-up attempts"
-        out[prec] = r
+        out[key] = r
         it.close()
-    out["speedup_mixed_vs_f64"] = (out["mixed"]["accepted_steps_per_s"] /
-                                   max(out["f64"]["accepted_steps_per_s"], 1e-30))
+    f64 = max(out["f64"]["accepted_steps_per_s"], 1e-30)
+    out["speedup_mixed_vs_f64"] = out["mixed"]["accepted_steps_per_s"] / f64
+    out["speedup_mixed_learned_vs_f64"] = out["mixed_learned"]["accepted_steps_per_s"] / f64
+    out["rhs_saved_learned_vs_reference"] = (1.0 - out["mixed_learned"]["rhs_evals"] /
+                                            max(out["mixed"]["rhs_evals"], 1))
     return out
 
 

@@ -227,6 +227,10 @@ CONFIGS = {
     # binary-rich Plummer spheres, DOPRI5, tol 1e-8
     "binary2048_dopri5": dict(ic="binary", n=2048, softening=1e-4, tab="DOPRI5", tol=1e-8,
                               tf=0.02, attempts=300),
+    # the single large system at tol 1e-11, where its relative energy error
+    # over t in [0, 2] is below 1e-8
+    "plummer16384_rkf78_tol1e-11": dict(ic="plummer", n=16384, softening=0.005, tab="RKF78",
+                                        tol=1e-11, tf=2.0, attempts=800),
 }
 SEEDS_A = list(range(1, 17))
 SEEDS_B = list(range(101, 117))
