@@ -36,3 +36,35 @@ def test_learned_proposer_gain_on_held_out_systems(gb, torch_cuda, capsys):
     # same trajectory to tolerance level
     assert gain["energy_err_ratio"] <= 3.0
     assert gain["max_state_diff_vs_reference"] <= 1e-2
+
+
+def test_shipped_tight_tolerance_proposer_saves_rhs(gb, torch_cuda):
+    """The proposer shipped for the headline system at tol 1e-11 (relative
+    energy error below 1e-8 over t in [0, 2]) takes fewer RHS evaluations than
+    the reference controller on held-out seeds, with both runs' energy error
+    below 1e-8."""
+    import os
+    from ode_prototyping_gb300 import learned
+    c = learned.CONFIGS["plummer16384_rkf78_tol1e-11"]
+    path = os.path.join(os.path.dirname(gb.__file__), "weights",
+                        "proposer_plummer16384_rkf78_tol1e-11.bin")
+    mlp = gb.GbMlp.from_buffer_copy(open(path, "rb").read())
+    n, eps, tol = c["n"], c["softening"], c["tol"]
+    rhs = {"reference": 0, "learned": 0}
+    for seed in learned.SEEDS_B[:2]:
+        x0 = gb.to_device(gb.ic_plummer(n, seed))
+        e0 = gb.energy(x0, n, eps, 1.0 / n)
+        for ctrl in rhs:
+            exe = gb.Gb300Executor(precision="mixed", controller=ctrl, attempts_per_sync=16,
+                                   mlp=mlp if ctrl == "learned" else None)
+            it = gb.Integrator(c["tab"], gb.NBodyODE(n, eps, 1.0 / n), exe)
+            it.start(x0, 0.0, c["tf"], tol, tol)
+            it.advance(0)
+            xs, t = it.state()
+            st = it.stats()
+            it.close()
+            assert t == c["tf"]
+            e1 = gb.energy(xs, n, eps, 1.0 / n)
+            assert abs(e1["e"] - e0["e"]) / abs(e0["e"]) <= 1e-8, (seed, ctrl)
+            rhs[ctrl] += st["n_rhs"]
+    assert rhs["learned"] < rhs["reference"], rhs
