@@ -1,8 +1,9 @@
 """CPU oracle for the adaptive embedded Runge-Kutta N-body path.
 
 Test infrastructure only.  The tests, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` import this package as the checker (or as the
-timed CPU implementation of the reference); the GPU library never does.
+CPU-baseline leg of ``bench.py`` import this package to compare the GPU results
+against (or as the timed CPU implementation of the reference); the GPU library
+never does.
 
 Two back ends:
 

@@ -2,8 +2,9 @@
  * gbode_oracle.c -- CPU oracle for the adaptive embedded Runge-Kutta N-body
  * path.  TEST INFRASTRUCTURE ONLY: the GPU library never links, loads or
  * calls anything in this file.  It is imported by the tests, by the smoke
- * check and by the CPU-baseline leg of bench.py, always as the checker (or as
- * the timed reference CPU implementation), never as the product.
+ * check and by the CPU-baseline leg of bench.py, always as the oracle the GPU
+ * results are compared against (or as the timed reference CPU implementation),
+ * never as the product.
  *
  * It is a plain-C restatement of the reference's algorithm, operation for
  * operation, so that with one thread it reproduces the reference's
