@@ -63,3 +63,30 @@ def test_reference_arm_runs_on_rank_zero_only(capsys):
     args = argparse.Namespace(gpus=2, steps=1, warmup=0)
     assert bench.run_reference(args, world=2, rank=1) is None  # returns without work
     assert capsys.readouterr().out == ""
+
+
+def test_stage_kernel_naming():
+    """The bench names the integrator's stage kernel from the geometry it
+    reports: one-lane packed mixed stages run as partner chunks
+    (fused_split_kernel), every other geometry as clusters."""
+    import bench
+    split = {"j_split": 16, "lanes": 1, "mixed_variant": 3}
+    assert bench.stage_kernel_name("mixed", split).startswith("fused_split_kernel")
+    assert "16 partner chunks" in bench.stage_kernel_name("mixed", split)
+    for geo in ({"j_split": 8, "lanes": 2, "mixed_variant": 3},   # clusters, lanes
+                {"j_split": 1, "lanes": 1, "mixed_variant": 3},   # one CTA per tile
+                {"j_split": 8, "lanes": 1, "mixed_variant": 1}):  # scalar loop
+        assert bench.stage_kernel_name("mixed", geo).startswith("fused_stage_kernel")
+    assert bench.stage_kernel_name("f64", split).startswith("fused_stage_kernel")
+
+
+def test_conservation_drift():
+    import numpy as np
+    import bench
+    e0 = {"e": -0.25, "p": np.zeros(3), "l": np.array([0.0, 0.0, 1.0])}
+    e1 = {"e": -0.25 * (1 + 2e-9), "p": np.array([3e-12, 0.0, 4e-12]),
+          "l": np.array([0.0, 0.0, 1.0 + 1e-11])}
+    d = bench.drift(e0, e1)
+    assert abs(d["energy_rel_err"] - 2e-9) < 1e-15
+    assert abs(d["momentum_drift"] - 5e-12) < 1e-20
+    assert abs(d["angular_momentum_drift"] - 1e-11) < 1e-16
