@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
                        const __grid_constant__ FusedParams P, int s) {
   static_assert(L == 1, "partner chunks: one lane per body");
   constexpr int BI = (T / L) * BPT;
-  constexpr int BW = BI * 3;  // doubles of one chunk's sums
+  constexpr int BW = BI * 3;  // sums of one chunk (8 bytes each)
   __shared__ __align__(16) unsigned char sh_raw[jp_smem_bytes<T>()];
   __shared__ double part[BI][3];
   __shared__ double red[T];
