@@ -64,3 +64,26 @@ def test_logs_are_concatenated_in_order():
     x, y = learned.build_dataset([a, b], q=4)
     assert len(y) == 1 + 2
     np.testing.assert_array_equal(x[1], b[0, :16].astype(np.float32))
+
+
+def test_shipped_weights_match_the_struct_and_a_configuration():
+    """Every shipped proposer is a raw gb_mlp of the current layout, named for
+    a training configuration, with finite weights, non-negative input scales
+    (0 switches off a feature that was constant in training) and a positive
+    output scale."""
+    import ctypes
+    import glob
+    import os
+    import ode_prototyping_gb300 as gb
+    files = sorted(glob.glob(os.path.join(os.path.dirname(gb.__file__), "weights", "*.bin")))
+    assert files
+    for path in files:
+        name = os.path.basename(path)[len("proposer_"):-len(".bin")]
+        assert name in learned.CONFIGS, name
+        raw = open(path, "rb").read()
+        assert len(raw) == ctypes.sizeof(gb.GbMlp), name
+        m = gb.GbMlp.from_buffer_copy(raw)
+        flat = np.frombuffer(raw, dtype=np.float32)
+        assert np.all(np.isfinite(flat)), name
+        assert all(s >= 0 for s in m.in_scale) and any(s > 0 for s in m.in_scale), name
+        assert m.out_scale > 0, name
