@@ -115,3 +115,37 @@ def test_mlp_init_host(gb):
     w1 = np.ctypeslib.as_array(m.w1)
     assert np.abs(w1).max() <= np.sqrt(6 / 80) + 1e-6 and np.abs(w1).std() > 0
     assert list(m.in_scale) == [1.0] * 16 and m.out_scale == 1.0
+
+
+def _header_enum(name):
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    m = re.search(r"\b" + name + r"\s*=\s*(\d+)", src)
+    assert m, name
+    return int(m.group(1))
+
+
+def test_binding_enums_match_header(gb):
+    assert gb.PREC == {"f64": _header_enum("GB_PREC_F64"), "mixed": _header_enum("GB_PREC_MIXED")}
+    assert gb.CONTROLLERS == {"reference": _header_enum("GB_CTRL_REFERENCE"),
+                              "pi": _header_enum("GB_CTRL_PI"),
+                              "learned": _header_enum("GB_CTRL_LEARNED")}
+
+
+def test_executor_options_reach_the_c_struct(gb):
+    """Gb300Executor -> gb_integrate_opts, field by field (no GPU)."""
+    mlp = gb.GbMlp()
+    exe = gb.Gb300Executor(precision="mixed", controller="learned", exact=False, fsal=False,
+                           attempts_per_sync=5, tile=gb.tiling(16, 1, 0, mixed_variant=3),
+                           max_attempts=77, pi_beta=0.06, mlp=mlp, log_steps=9,
+                           spatial_sort=True, host_wait_timeout_s=1.5)
+    o = exe.opts(record=True)
+    assert (o.precision, o.controller, o.fsal, o.exact) == (1, 2, 0, 0)
+    assert (o.attempts_per_sync, o.record, o.max_attempts, o.log_steps, o.spatial_sort) == \
+        (5, 1, 77, 9, 1)
+    assert o.pi_beta == 0.06 and o.host_wait_timeout_s == 1.5
+    assert (o.tiling.j_split, o.tiling.lanes, o.tiling.bodies_per_cta,
+            o.tiling.mixed_variant) == (16, 1, 0, 3)
+    assert o.mlp == C.addressof(mlp)
+    d = gb.Gb300Executor().opts(record=False)
+    assert (d.precision, d.controller, d.fsal, d.exact, d.record, d.mlp) == (0, 0, 1, 0, 0, None)
+    assert gb.tiling(scalar=True).mixed_variant == 1
