@@ -160,7 +160,11 @@ int gb_nbody_rhs_mixed_sorted(const double* x_dev, double* dxdt_dev, int64_t n_p
 /* device address up (cudaGetSymbolAddress); make that first call before   */
 /* any stream capture.  All calls share the one array, so calls that       */
 /* overlap on the GPU (other streams, other threads) race and must be      */
-/* serialised by the caller.  Nothing in it needs to start at zero.        */
+/* serialised by the caller.  Nothing in it needs to start at zero.  The  */
+/* looked-up address is kept for the life of the process: after           */
+/* cudaDeviceReset the module is reloaded at a possibly different address, */
+/* so this entry point must not be called after a reset.  It checks its    */
+/* arguments as gb_nbody_rhs_mixed does and gives the same bits.           */
 int64_t gb_nbody_rhs_mixed_noalloc_max_bodies(void);
 int gb_nbody_rhs_mixed_noalloc(const double* x_dev, double* dxdt_dev, int64_t n_particles,
                                double softening, double mass, const double* masses_dev,

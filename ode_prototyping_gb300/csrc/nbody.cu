@@ -8,6 +8,16 @@
 
 namespace gb {
 
+// Argument checks shared by the right-hand-side entry points (also the
+// allocation-free one in noalloc.cu).
+int validate_nbody(const void* a, const void* b, long long n, double softening, double mass,
+                   const double* masses) {
+  if (!a || !b || n < 1) return GB_ERR_INVALID_ARGUMENT;
+  if (!(softening >= 0.0) || !std::isfinite(softening)) return GB_ERR_INVALID_ARGUMENT;
+  if (!masses && !(mass > 0.0)) return GB_ERR_INVALID_ARGUMENT;
+  return GB_OK;
+}
+
 namespace {
 
 enum { kModeRhs = 0, kModeAccWrite = 1, kModeAccAdd = 2 };
@@ -156,14 +166,6 @@ const void* pick_mixed(int L, int BPT, bool packed = false) {
 // scalar loop (mixed_variant == 1).
 bool use_packed(const gb_force_tiling* tiling, int BPT, const double* masses) {
   return (BPT == 1 || BPT == 2) && !masses && !(tiling && tiling->mixed_variant == 1);
-}
-
-int validate_nbody(const void* a, const void* b, long long n, double softening, double mass,
-                   const double* masses) {
-  if (!a || !b || n < 1) return GB_ERR_INVALID_ARGUMENT;
-  if (!(softening >= 0.0) || !std::isfinite(softening)) return GB_ERR_INVALID_ARGUMENT;
-  if (!masses && !(mass > 0.0)) return GB_ERR_INVALID_ARGUMENT;
-  return GB_OK;
 }
 
 int run_f64(const double* pos, const double* vel, double* out_vel, double* out_acc, long long n,
@@ -336,8 +338,10 @@ extern "C" int gb_nbody_acc_f64(const double* pos, double* acc, int64_t n, doubl
 
 namespace gb {
 // Mixed-precision right-hand side into caller-located scratch: `packed`
-// (n PackedBody records, 16-byte aligned) and `c` (3 doubles).  Same kernels
-// and launch geometry as gb_nbody_rhs_mixed; allocates nothing.
+// (n PackedBody records, 16-byte aligned) and `c` (3 doubles).  Both
+// gb_nbody_rhs_mixed (workspace from the caller) and
+// gb_nbody_rhs_mixed_noalloc (workspace inside the library) run through it,
+// so the two give identical bits; allocates nothing.
 int mixed_rhs_into(const double* x, double* dxdt, long long n, double softening, double mass,
                    const double* masses, PackedBody* packed, double* c,
                    const gb_force_tiling* tiling, cudaStream_t s) {
@@ -492,29 +496,8 @@ extern "C" int gb_nbody_rhs_mixed(const double* x, double* dxdt, int64_t n, doub
   GB_TRY(validate_nbody(x, dxdt, n, softening, mass, masses));
   if (!work || (reinterpret_cast<uintptr_t>(work) & 15u)) return GB_ERR_INVALID_ARGUMENT;
   if (!(softening > 0.0)) return GB_ERR_INVALID_ARGUMENT;
-  cudaStream_t s = as_cuda(stream);
   PackedBody* packed = reinterpret_cast<PackedBody*>(work);
-  size_t packed_bytes = ((size_t)n * sizeof(PackedBody) + 255) / 256 * 256;
+  const size_t packed_bytes = ((size_t)n * sizeof(PackedBody) + 255) / 256 * 256;
   double* c = reinterpret_cast<double*>(reinterpret_cast<char*>(work) + packed_bytes);
-  centroid_kernel<<<1, 1024, 0, s>>>(x, n, c);
-  GB_CUDA_TRY(cudaGetLastError());
-  pack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, masses, c, n, packed);
-  GB_CUDA_TRY(cudaGetLastError());
-  ForceGeom g = choose_geom(n, GB_PREC_MIXED, tiling, 0, masses == nullptr);
-  const void* k = nullptr;
-  switch (g.T) {
-    case 64: k = pick_mixed<64>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
-    case 128: k = pick_mixed<128>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
-    case 256: k = pick_mixed<256>(g.L, g.BPT, use_packed(tiling, g.BPT, masses)); break;
-  }
-  if (!k) return GB_ERR_UNSUPPORTED;
-  const double* vel = x + 3 * n;
-  double* out_vel = dxdt;
-  double* out_acc = dxdt + 3 * n;
-  float eps2 = (float)(softening * softening);
-  int uniform = masses ? 0 : 1;
-  long long nn = n;
-  void* args[] = {(void*)&packed, (void*)&vel,  (void*)&out_vel, (void*)&out_acc,
-                  (void*)&nn,     (void*)&eps2, (void*)&mass,    (void*)&uniform};
-  return launch_cluster(k, g, 0, s, args);
+  return mixed_rhs_into(x, dxdt, n, softening, mass, masses, packed, c, tiling, as_cuda(stream));
 }

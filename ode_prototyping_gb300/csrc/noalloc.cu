@@ -15,6 +15,8 @@
 #include "force.cuh"
 
 namespace gb {
+int validate_nbody(const void* a, const void* b, long long n, double softening, double mass,
+                   const double* masses);
 int mixed_rhs_into(const double* x, double* dxdt, long long n, double softening, double mass,
                    const double* masses, PackedBody* packed, double* c,
                    const gb_force_tiling* tiling, cudaStream_t s);
@@ -35,6 +37,9 @@ void* g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device, looked up once
 // per device (the host-side name of a __device__ array is only a stand-in).
+// The cached address belongs to the device's current context: after
+// cudaDeviceReset the module is loaded again and the address may change, so
+// this entry point must not be called after a reset in the same process.
 int scratch_for_current_device(unsigned char** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -64,8 +69,9 @@ extern "C" int64_t gb_nbody_rhs_mixed_noalloc_max_bodies(void) { return kNoAlloc
 extern "C" int gb_nbody_rhs_mixed_noalloc(const double* x, double* dxdt, int64_t n,
                                           double softening, double mass, const double* masses,
                                           const gb_force_tiling* tiling, gb_stream_t stream) {
-  if (!x || !dxdt || n < 1) return GB_ERR_INVALID_ARGUMENT;
-  if (!(softening > 0.0) || (!masses && !(mass > 0.0))) return GB_ERR_INVALID_ARGUMENT;
+  // the same argument checks as gb_nbody_rhs_mixed
+  GB_TRY(gb::validate_nbody(x, dxdt, n, softening, mass, masses));
+  if (!(softening > 0.0)) return GB_ERR_INVALID_ARGUMENT;
   if (n > kNoAllocMaxBodies) return GB_ERR_CAPACITY;
   unsigned char* base = nullptr;
   int rc = scratch_for_current_device(&base);

@@ -25,6 +25,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
+# Where the reference's sources are read from (this container only; they do
+# not travel to the GPU machine).  Every recipe and test takes it from here.
 REF_ROOT = os.environ.get("GBODE_REFERENCE_ROOT", "/root/reference")
 
 TABLEAUS = {"HE21": 0, "RKF45": 1, "DOPRI5": 2, "DVERK": 3, "RKF78": 4}
@@ -106,6 +108,13 @@ def lib() -> C.CDLL:
                                       C.POINTER(C.c_int64)]
         _lib.orc_spinning_cube.argtypes = [C.c_int64, C.c_double, C.c_uint32, _DP]
         _lib.orc_tableau_builtin.argtypes = [C.c_int, C.POINTER(Tableau)]
+        _lib.orc_dopri5_dense_eval.argtypes = [_DP, _DP, _DP, C.c_int64, C.c_double,
+                                               C.c_double, _DP, C.c_int64, _DP]
+        _lib.orc_pi_sequence.argtypes = [C.c_double] * 5 + [_DP, C.c_int64, C.c_double, _DP]
+        _lib.orc_session_set_controller.argtypes = [C.c_void_p, C.c_int, C.c_double]
+        _lib.orc_session_set_dense.argtypes = [C.c_void_p, _DP, C.c_int64, _DP]
+        _lib.orc_session_dense_count.argtypes = [C.c_void_p]
+        _lib.orc_session_dense_count.restype = C.c_int64
         for name in ("orc_sizeof_tableau", "orc_sizeof_ode", "orc_sizeof_stats"):
             getattr(_lib, name).restype = C.c_size_t
         assert _lib.orc_sizeof_tableau() == C.sizeof(Tableau)
@@ -131,7 +140,51 @@ def ref() -> C.CDLL:
         _ref.ref_nbody_rhs.argtypes = [C.c_int64, C.c_double, C.c_double, C.c_int, _DP, _DP,
                                        C.c_int64]
         _ref.ref_nbody_sizes.argtypes = [C.POINTER(C.c_int64), C.c_int]
+        _ref.ref_nr_dopr5_dense.argtypes = [C.c_int64, _DP, _DP, _DP, C.c_double, C.c_double,
+                                            _DP, C.c_int64, _DP]
+        _ref.ref_nr_dopr5_controller.argtypes = [_DP, C.c_int64, C.c_double, _DP]
     return _ref
+
+
+def ref_dopri5_dense(y0, y1, ks, h: float, t_new: float, ts) -> np.ndarray:
+    """The reference's own DOPRI5 dense output (Numerical Recipes'
+    prepare_dense / dense_out, compiled in place)."""
+    y0, y1, ks, ts = (np.ascontiguousarray(a, dtype=np.float64) for a in (y0, y1, ks, ts))
+    n = len(y0)
+    out = np.zeros((len(ts), n))
+    assert ref().ref_nr_dopr5_dense(n, _ptr(y0), _ptr(y1), _ptr(ks), h, t_new, _ptr(ts),
+                                    len(ts), _ptr(out)) == 0
+    return out
+
+
+def ref_dopri5_controller(errs, h0: float) -> np.ndarray:
+    """The reference's Controller::success (Numerical Recipes' DOPRI5
+    stepper, compiled in place) on a sequence of error norms."""
+    errs = np.ascontiguousarray(errs, dtype=np.float64)
+    hs = np.zeros(len(errs))
+    assert ref().ref_nr_dopr5_controller(_ptr(errs), len(errs), h0, _ptr(hs)) == 0
+    return hs
+
+
+def dopri5_dense(y0, y1, ks, h: float, t_new: float, ts) -> np.ndarray:
+    """The restated DOPRI5 dense output (gbode_oracle.c orc_dopri5_dense)."""
+    y0, y1, ks, ts = (np.ascontiguousarray(a, dtype=np.float64) for a in (y0, y1, ks, ts))
+    n = len(y0)
+    out = np.zeros((len(ts), n))
+    assert lib().orc_dopri5_dense_eval(_ptr(y0), _ptr(y1), _ptr(ks), n, h, t_new, _ptr(ts),
+                                       len(ts), _ptr(out)) == 0
+    return out
+
+
+def pi_sequence(safe: float, alpha: float, beta: float, minscale: float, maxscale: float,
+                errs, h0: float) -> np.ndarray:
+    """The restated PI controller (gbode_oracle.c orc_pi_scale) with explicit
+    constants on a sequence of error norms: the step after each decision."""
+    errs = np.ascontiguousarray(errs, dtype=np.float64)
+    hs = np.zeros(len(errs))
+    assert lib().orc_pi_sequence(safe, alpha, beta, minscale, maxscale, _ptr(errs), len(errs),
+                                 h0, _ptr(hs)) == 0
+    return hs
 
 
 def ref_sizes() -> list[int]:
@@ -324,7 +377,8 @@ class Session:
     timing the reference's CPU implementation on bounded samples."""
 
     def __init__(self, tab: str, ode: Ode, x0, t0: float, tf: float, atol, rtol,
-                 n_threads: int = 1):
+                 n_threads: int = 1, controller: str = "reference", pi_beta: float = 0.04,
+                 dense_times=None):
         L = lib()
         if not getattr(L, "_session_bound", False):
             L.orc_session_create.restype = C.c_void_p
@@ -347,6 +401,16 @@ class Session:
                                       _ptr(self._a), _ptr(self._r), n_threads)
         assert self.h
         self.n_var = n_var
+        if controller == "pi":
+            assert L.orc_session_set_controller(self.h, 1, pi_beta) == 0
+        else:
+            assert controller == "reference", controller
+        self._dense_t = None
+        if dense_times is not None:
+            self._dense_t = np.ascontiguousarray(dense_times, dtype=np.float64)
+            self._dense = np.zeros((len(self._dense_t), n_var))
+            assert L.orc_session_set_dense(self.h, _ptr(self._dense_t), len(self._dense_t),
+                                           _ptr(self._dense)) == 0
 
     def attempt(self) -> tuple[bool, bool]:
         acc = C.c_int(0)
@@ -357,6 +421,27 @@ class Session:
         st = Stats()
         lib().orc_session_stats(self.h, C.byref(st))
         return {f: getattr(st, f) for f, _ in Stats._fields_}
+
+    def dense(self) -> np.ndarray:
+        """Dense outputs produced so far (DOPRI5 sessions with dense_times)."""
+        if self._dense_t is None:
+            return np.zeros((0, self.n_var))
+        return self._dense[: int(lib().orc_session_dense_count(self.h))].copy()
+
+    def run(self):
+        """Attempts until t reaches tf: (times, states) of t0 and every
+        accepted step, as the reference's RawOutput records them."""
+        x, t = self.state()
+        times, states = [t], [x]
+        while True:
+            done, acc = self.attempt()
+            if done:
+                break
+            if acc:
+                x, t = self.state()
+                times.append(t)
+                states.append(x)
+        return np.array(times), np.array(states)
 
     def state(self):
         t = C.c_double(0)

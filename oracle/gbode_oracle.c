@@ -608,6 +608,38 @@ static double orc_estimate_initial_step(orc_pool* pool, const orc_tableau* bt,
   return dt1 < big ? dt1 : big;
 }
 
+/* PI step-size controller, restating NumericalRecipes/StepperDopr5.hpp:
+ * 236-272 (Controller::success) with its constants as parameters: on an
+ * accepted step scale = safe * err^-alpha * errold^beta (maxscale when
+ * err == 0), clamped to [minscale, maxscale], no increase right after a
+ * rejection, errold = max(err, 1e-4); a rejection scales by
+ * max(safe * err^-alpha, minscale).  Returns the factor applied to h. */
+typedef struct {
+  double safe, alpha, beta, minscale, maxscale, errold;
+  int reject;
+} orc_pi;
+
+static double orc_pi_scale(orc_pi* c, double err, int accepted) {
+  double scale;
+  if (accepted) {
+    if (err == 0.0) {
+      scale = c->maxscale;
+    } else {
+      scale = c->safe * pow(err, -c->alpha) * pow(c->errold, c->beta);
+      if (scale < c->minscale) scale = c->minscale;
+      if (scale > c->maxscale) scale = c->maxscale;
+    }
+    if (c->reject && scale > 1.0) scale = 1.0;
+    c->errold = err > 1.0e-4 ? err : 1.0e-4;
+    c->reject = 0;
+  } else {
+    scale = c->safe * pow(err, -c->alpha);
+    if (scale < c->minscale) scale = c->minscale;
+    c->reject = 1;
+  }
+  return scale;
+}
+
 /* Resumable form of the reference's adaptive loop: a session holds the
  * loop state (t, dt, x0, buffers, executor) of RKEmbeddedParallel::integrate
  * so that attempts can be run and timed one at a time. */
@@ -621,7 +653,74 @@ typedef struct {
   double *x0, *x, *ks, *temp, *err, *target, *atol, *rtol;
   orc_rk_ctx c;
   orc_stats st;
+  /* step-size controller: 0 = the reference's elementary controller
+   * (RKEmbeddedParallel.hpp:65-74), 1 = PI (orc_pi_step) */
+  int controller;
+  orc_pi pi;
+  /* DOPRI5 dense output: outputs at dense_t[0..n_dense) (ascending) into
+   * dense_out[j * n_var ...]; dense_next = first output not yet produced */
+  const double* dense_t;
+  double* dense_out;
+  int64_t n_dense, dense_next;
 } orc_session;
+
+/* The controller alone on a sequence of error norms (accepted iff err <= 1,
+ * as in Controller::success), starting from step h0: hs[k] = the step after
+ * the k-th decision (hnext on success, the reduced h on a rejection).  Used
+ * to pin orc_pi_scale to the reference's own Controller::success. */
+int orc_pi_sequence(double safe, double alpha, double beta, double minscale, double maxscale,
+                    const double* errs, int64_t n, double h0, double* hs) {
+  if (!errs || !hs || n < 0) return -1;
+  orc_pi c = {safe, alpha, beta, minscale, maxscale, 1.0e-4, 0};
+  double h = h0;
+  for (int64_t k = 0; k < n; ++k) {
+    const double scale = orc_pi_scale(&c, errs[k], errs[k] <= 1.0);
+    h = h * scale;
+    hs[k] = h;
+  }
+  return 0;
+}
+
+/* The session's PI controller (GB_CTRL_PI on the GPU): orc_pi_scale with
+ * the reference integrator's constants instead of Numerical Recipes' (safe =
+ * 0.38^(1/(1+q)), minscale 0.33, maxscale 6, RKEmbeddedParallel.hpp:21-24;
+ * alpha = 1/(1+q) - 0.75 beta), and the reference's floor on the new step
+ * at (tf - t0) * 1e-12 (:71-72). */
+static double orc_pi_step(orc_session* ss, double dt, double err, int accepted) {
+  double dtn = dt * orc_pi_scale(&ss->pi, err, accepted);
+  if (dtn / (ss->tf - ss->t0) < 1.0e-12) dtn = (ss->tf - ss->t0) * 1.0e-12;
+  return dtn;
+}
+
+/* DOPRI5 dense output over the step just accepted (y0 at t_old, y1 at
+ * t_old + h), restating NumericalRecipes/StepperDopr5.hpp:179-219:
+ * prepare_dense's rcont1..5 from y0, y1 and the stage derivatives k1, k3..k7
+ * (k7 = f(y1), the seventh stage), then dense_out's polynomial in
+ * s = (t - (t_new - h)) / h. */
+static void orc_dopri5_dense(const double* y0, const double* y1, const double* ks, int64_t n,
+                             double h, double t_new, const double* ts, int64_t nt,
+                             double* out) {
+  const double d1 = -12715105075.0 / 11282082432.0, d3 = 87487479700.0 / 32700410799.0,
+               d4 = -10690763975.0 / 1880347072.0, d5 = 701980252875.0 / 199316789632.0,
+               d6 = -1453857185.0 / 822651844.0, d7 = 69997945.0 / 29380423.0;
+  const double *k1 = ks, *k3 = ks + 2 * n, *k4 = ks + 3 * n, *k5 = ks + 4 * n,
+               *k6 = ks + 5 * n, *k7 = ks + 6 * n;
+  for (int64_t i = 0; i < n; ++i) {
+    const double r1 = y0[i];
+    const double ydiff = y1[i] - y0[i];
+    const double r2 = ydiff;
+    const double bspl = h * k1[i] - ydiff;
+    const double r3 = bspl;
+    const double r4 = ydiff - h * k7[i] - bspl;
+    const double r5 =
+        h * (d1 * k1[i] + d3 * k3[i] + d4 * k4[i] + d5 * k5[i] + d6 * k6[i] + d7 * k7[i]);
+    for (int64_t j = 0; j < nt; ++j) {
+      const double sv = (ts[j] - (t_new - h)) / h;
+      const double s1 = 1.0 - sv;
+      out[j * n + i] = r1 + sv * (r2 + s1 * (r3 + sv * (r4 + s1 * r5)));
+    }
+  }
+}
 
 orc_session* orc_session_create(const orc_tableau* bt, const orc_ode* ode, const double* x0_in,
                                 double t0, double tf, const double* atol, const double* rtol,
@@ -697,19 +796,31 @@ int orc_session_attempt(orc_session* ss, int* accepted) {
   int acc = scaled_error <= 1.0;
   if (acc) {
     ss->t += dt;
+    if (ss->dense_out && S == 7) {
+      int64_t j1 = ss->dense_next;
+      while (j1 < ss->n_dense && ss->dense_t[j1] <= ss->t) ++j1;
+      if (j1 > ss->dense_next)
+        orc_dopri5_dense(ss->x0, ss->x, ss->ks, n_var, dt, ss->t, ss->dense_t + ss->dense_next,
+                         j1 - ss->dense_next, ss->dense_out + ss->dense_next * n_var);
+      ss->dense_next = j1;
+    }
     memcpy(ss->x0, ss->x, (size_t)n_var * sizeof(double));
   } else {
     ss->st.n_rejected++;
   }
-  double dtnew = dt * ss->safety_factor / pow(scaled_error, 1.0 / (1.0 + ss->q));
-  if (fabs(dtnew) > 6.0 * fabs(dt)) {
-    dt *= 6.0;
-  } else if (fabs(dtnew) < 0.33 * fabs(dt)) {
-    dt *= 0.33;
-  } else if (dtnew / (ss->tf - ss->t0) < 1.0e-12) {
-    dt = (ss->tf - ss->t0) * 1.0e-12;
+  if (ss->controller == 1) {
+    dt = orc_pi_step(ss, dt, scaled_error, acc);
   } else {
-    dt = dtnew;
+    double dtnew = dt * ss->safety_factor / pow(scaled_error, 1.0 / (1.0 + ss->q));
+    if (fabs(dtnew) > 6.0 * fabs(dt)) {
+      dt *= 6.0;
+    } else if (fabs(dtnew) < 0.33 * fabs(dt)) {
+      dt *= 0.33;
+    } else if (dtnew / (ss->tf - ss->t0) < 1.0e-12) {
+      dt = (ss->tf - ss->t0) * 1.0e-12;
+    } else {
+      dt = dtnew;
+    }
   }
   if (ss->t + dt > ss->tf) dt = ss->tf - ss->t;
   ss->dt = dt;
@@ -717,6 +828,42 @@ int orc_session_attempt(orc_session* ss, int* accepted) {
   if (accepted) *accepted = acc;
   return 0;
 }
+
+/* The dense formula alone (for pinning it to the reference's own
+ * prepare_dense / dense_out): ks holds the seven stage derivatives
+ * stage-major (ks[j * n + i]). */
+int orc_dopri5_dense_eval(const double* y0, const double* y1, const double* ks, int64_t n,
+                          double h, double t_new, const double* ts, int64_t nt, double* out) {
+  if (!y0 || !y1 || !ks || !ts || !out || n < 0 || nt < 0 || !(h != 0.0)) return -1;
+  orc_dopri5_dense(y0, y1, ks, n, h, t_new, ts, nt, out);
+  return 0;
+}
+
+/* Switches the session's step-size controller: kind 0 = the reference's
+ * elementary controller, 1 = PI with the given beta (alpha = 1/(1+q) -
+ * 0.75 beta, errold starting at 1e-4).  Call before the first attempt. */
+int orc_session_set_controller(orc_session* ss, int kind, double beta) {
+  if (!ss || (kind != 0 && kind != 1)) return -1;
+  ss->controller = kind;
+  orc_pi c = {ss->safety_factor, 1.0 / (1.0 + ss->q) - 0.75 * beta, beta, 0.33, 6.0, 1.0e-4, 0};
+  ss->pi = c;
+  return 0;
+}
+
+/* DOPRI5 dense output at the ascending times ts[0..nt) into out[nt][n_var]
+ * (caller-owned, kept alive while the session runs).  Returns -1 unless the
+ * session's tableau has seven stages (DOPRI5). */
+int orc_session_set_dense(orc_session* ss, const double* ts, int64_t nt, double* out) {
+  if (!ss || ss->bt.n_stages != 7 || nt < 0 || (nt > 0 && (!ts || !out))) return -1;
+  ss->dense_t = ts;
+  ss->dense_out = out;
+  ss->n_dense = nt;
+  ss->dense_next = 0;
+  return 0;
+}
+
+/* Number of dense outputs produced so far. */
+int64_t orc_session_dense_count(const orc_session* ss) { return ss ? ss->dense_next : 0; }
 
 const double* orc_session_state(const orc_session* ss, double* t) {
   if (t) *t = ss->t;

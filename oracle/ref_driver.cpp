@@ -24,6 +24,7 @@
 #include "ParallelExecutor.hpp"
 #include "RKEmbeddedParallel.hpp"
 #include "RawOutput.hpp"
+#include "StepperDopr5.hpp"
 #include "SingleThreadedExecutor.hpp"
 #include "ThreadPoolExecutor.hpp"
 #include "VanDerPolODE.hpp"
@@ -133,6 +134,15 @@ int nbody_rhs(double softening, double mass, int n_threads, double const* x, dou
   return 0;
 }
 
+// Stand-ins for the derivative functor and output policy of the Numerical
+// Recipes DOPRI5 stepper; only prepare_dense, dense_out and
+// Controller::success are called, which use neither.
+struct NoDerivs {
+  void operator()(double, std::vector<double>&, std::vector<double>&) {}
+};
+struct NoSave {};
+using NrDopr5 = StepperDopr5<NoDerivs, NoSave>;
+
 #define GB_REF_SIZES(X) X(5) X(16) X(64) X(128) X(256) X(1024) X(4096) X(16384)
 
 }  // namespace
@@ -199,6 +209,43 @@ int ref_nbody_rhs(std::int64_t n_particles, double softening, double mass, int n
 #undef GB_CASE
     default: return -1;
   }
+}
+
+// The reference's DOPRI5 dense output (NumericalRecipes/StepperDopr5.hpp:
+// 179-219): prepare_dense from y0 (at t_new - h), y1 (at t_new) and the seven
+// stage derivatives ks[j * n + i], then dense_out at each time ts[k] into
+// out[k * n + i].
+int ref_nr_dopr5_dense(std::int64_t n, double const* y0, double const* y1, double const* ks,
+                       double h, double t_new, double const* ts, std::int64_t nt, double* out) {
+  std::vector<double> y(y0, y0 + n), dydx(ks, ks + n);
+  double x = t_new;
+  NoDerivs d;
+  NrDopr5 st(y, dydx, x, 0.0, 0.0, d);
+  st.yout.assign(y1, y1 + n);
+  st.k3.assign(ks + 2 * n, ks + 3 * n);
+  st.k4.assign(ks + 3 * n, ks + 4 * n);
+  st.k5.assign(ks + 4 * n, ks + 5 * n);
+  st.k6.assign(ks + 5 * n, ks + 6 * n);
+  st.dydxnew.assign(ks + 6 * n, ks + 7 * n);
+  Dopr5DenseData dd;
+  st.prepare_dense(h, dd);
+  for (std::int64_t k = 0; k < nt; ++k)
+    for (std::int64_t i = 0; i < n; ++i) out[k * n + i] = st.dense_out((int)i, ts[k], h, dd);
+  return 0;
+}
+
+// The reference's step-size controller (Controller::success,
+// NumericalRecipes/StepperDopr5.hpp:236-272) on a sequence of error norms,
+// as StepperDopr5::step drives it: after a success the next step is hnext,
+// after a rejection the reduced h.  hs[k] = the step after decision k.
+int ref_nr_dopr5_controller(double const* errs, std::int64_t m, double h0, double* hs) {
+  NrDopr5::Controller con;
+  double h = h0;
+  for (std::int64_t k = 0; k < m; ++k) {
+    if (con.success(errs[k], h)) h = con.hnext;
+    hs[k] = h;
+  }
+  return 0;
 }
 
 }  // extern "C"

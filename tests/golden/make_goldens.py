@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 
 import oracle as O  # noqa: E402
 
-REF = os.environ.get("GBODE_REFERENCE_ROOT", "/root/reference")
+REF = O.REF_ROOT
 TEST_CPP = os.path.join(REF, "src/test/SingleThreadedRKEmbeddedTest.cpp")
 
 

@@ -6,11 +6,12 @@ import subprocess
 
 import pytest
 
+import oracle
 from conftest import ROOT
 
 INC = os.path.join(ROOT, "include")
 CPP = os.path.join(ROOT, "tests", "cpp")
-REF = os.environ.get("GBODE_REFERENCE_ROOT", "/root/reference")
+REF = oracle.REF_ROOT
 
 
 def _gxx(args):

@@ -232,6 +232,56 @@ def test_pi_controller_runs(gb, torch_cuda):
     assert np.max(np.abs(s_pi[-1] - s_ref[-1])) <= 1e-7
 
 
+@pytest.mark.parametrize("tab,n,soft,tf,beta", [("DOPRI5", 64, 0.05, 0.5, 0.04),
+                                                ("RKF78", 128, 0.02, 0.3, 0.04),
+                                                ("DOPRI5", 100, 0.03, 0.4, 0.08)])
+def test_pi_controller_matches_oracle(gb, orc, torch_cuda, tab, n, soft, tf, beta):
+    """The device PI controller against the oracle's restatement of
+    Controller::success (NumericalRecipes/StepperDopr5.hpp:236-272 with the
+    reference integrator's constants, pinned to the reference's own
+    controller on the CPU): same accepted-step count, final state within
+    10x the tolerance (exact mode: serial pair sums, as the oracle)."""
+    x0 = gb.ic_plummer(n, 17)
+    tol = 1e-9
+    times, states, st = run(gb, tab, n, soft, 1.0 / n, x0, 0.0, tf, tol, controller="pi",
+                            pi_beta=beta, exact=True)
+    ode, _ = orc.nbody_ode(n, soft, 1.0 / n)
+    s = orc.Session(tab, ode, x0, 0.0, tf, tol, tol, controller="pi", pi_beta=beta)
+    o_times, o_states = s.run()
+    o_st = s.stats()
+    s.close()
+    assert len(times) == len(o_times)
+    assert st["n_rejected"] == o_st["n_rejected"]
+    assert times[-1] == o_times[-1] == tf
+    assert np.max(np.abs(states[-1] - o_states[-1])) <= 10 * tol
+
+
+def test_dopri5_dense_output_matches_oracle(gb, orc, torch_cuda):
+    """Dense output on the device against the oracle's restatement of
+    prepare_dense / dense_out (NumericalRecipes/StepperDopr5.hpp:179-219,
+    pinned bit for bit to the reference's own code on the CPU) on the same
+    accepted steps (exact mode: the trajectory is the reference's, bit for
+    bit): every output within 1e-12 of the oracle's, relative to the state."""
+    n, soft, tol, tf = 64, 0.05, 1e-9, 0.3
+    x0 = gb.ic_plummer(n, 21)
+    ode = gb.NBodyODE(n, soft, 1.0 / n)
+    times = np.sort(np.concatenate([np.linspace(0.013, 0.29, 17), [0.3]]))
+    it = gb.Integrator("DOPRI5", ode, gb.Gb300Executor(exact=True, attempts_per_sync=4))
+    it.set_dense_output(times)
+    it.start(x0, 0.0, tf, tol, tol)
+    assert it.advance(0) == 0
+    dense = it.dense_output()
+    it.close()
+    ode_o, _ = orc.nbody_ode(n, soft, 1.0 / n)
+    s = orc.Session("DOPRI5", ode_o, x0, 0.0, tf, tol, tol, dense_times=times)
+    s.run()
+    o_dense = s.dense()
+    s.close()
+    assert dense.shape == o_dense.shape == (len(times), 6 * n)
+    scale = np.max(np.abs(o_dense), axis=1, keepdims=True)
+    assert np.max(np.abs(dense - o_dense) / scale) <= 1e-12
+
+
 def test_enqueue_and_state(gb, torch_cuda):
     n = 128
     x0 = gb.ic_plummer(n, 2)

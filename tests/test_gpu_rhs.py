@@ -48,6 +48,24 @@ def test_rhs_f64_tilings_within_1e12(gb, orc, torch_cuda, P, L, B):
     np.testing.assert_array_equal(got[: 3 * n], ref[: 3 * n])
 
 
+@pytest.mark.parametrize("n,soft,gen,rows", [(16384, 0.005, "plummer", 4096),
+                                             (262144, 0.002, "cold", 1024)])
+def test_rhs_f64_config_sizes_sampled_rows(gb, orc, torch_cuda, n, soft, gen, rows):
+    """The FP64 right-hand side at the configurations' sizes with the default
+    launch geometry (at N = 16384: 8 cluster ranks x 2 lanes; at 262144: 8 x 1)
+    against the oracle's pair sum (NBodyODE.hpp:68-133 restated) on sampled
+    rows: <= 1e-12 relative per body, velocities copied exactly."""
+    x = gb.ic_plummer(n, 101) if gen == "plummer" else gb.ic_cold_sphere(n, 5, 0.01)
+    got = gb.nbody_rhs_f64(x, n, soft, 1.0 / n).cpu().numpy()
+    np.testing.assert_array_equal(got[: 3 * n], x[3 * n:])
+    sel = np.sort(np.random.default_rng(n).choice(n, rows, replace=False))
+    ode, _ = orc.nbody_ode(n, soft, 1.0 / n)
+    ref = orc.acc_rows(ode, x, sel)
+    a = got[3 * n:].reshape(-1, 3)[sel]
+    rel = np.linalg.norm(a - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert rel.max() <= 1e-12, rel.max()
+
+
 def test_rhs_f64_deterministic(gb, torch_cuda):
     n = 2048
     x = _x(n, 3)

@@ -132,3 +132,98 @@ def test_reference_build_agrees_when_present(orc):
     r2 = orc.ref_integrate_nbody("DOPRI5", 16, 0.5, 1 / 16, x, 0.0, 0.1, 1e-9, 1e-9)
     np.testing.assert_array_equal(r1.times, r2.times)
     np.testing.assert_array_equal(r1.states, r2.states)
+
+
+def _need_ref(orc):
+    if not orc.ref_available():
+        pytest.skip("reference not compiled in place (oracle/_ref)")
+
+
+def test_pi_controller_pinned_to_reference(orc):
+    """The restated PI controller with Numerical Recipes' constants (safe
+    0.9, alpha 0.2, beta 0, scale in [0.2, 10]) reproduces the reference's
+    own Controller::success (NumericalRecipes/StepperDopr5.hpp:236-272,
+    compiled in place) bit for bit on a sequence of error norms with
+    successes, rejections, repeated rejections and a zero error."""
+    _need_ref(orc)
+    rng = np.random.default_rng(5)
+    errs = np.concatenate([rng.uniform(0.01, 3.0, 200), [0.0, 2.5, 7.0, 0.3, 1e-9, 1.0, 1.0 + 1e-15,
+                                                         50.0, 0.999, 1e-3]])
+    got = orc.pi_sequence(0.9, 0.2, 0.0, 0.2, 10.0, errs, 1e-3)
+    ref = orc.ref_dopri5_controller(errs, 1e-3)
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_dopri5_dense_pinned_to_reference(orc):
+    """The restated DOPRI5 dense output reproduces the reference's own
+    prepare_dense / dense_out (NumericalRecipes/StepperDopr5.hpp:179-219,
+    compiled in place) bit for bit, at interior points and both ends."""
+    _need_ref(orc)
+    rng = np.random.default_rng(6)
+    n = 37
+    y0, y1 = rng.standard_normal(n), rng.standard_normal(n)
+    ks = rng.standard_normal(7 * n)
+    h, t_new = 0.0137, 2.5
+    ts = np.concatenate([[t_new - h], np.sort(rng.uniform(t_new - h, t_new, 9)), [t_new]])
+    np.testing.assert_array_equal(orc.dopri5_dense(y0, y1, ks, h, t_new, ts),
+                                  orc.ref_dopri5_dense(y0, y1, ks, h, t_new, ts))
+
+
+def test_pi_session_integrates_reference_problems(orc):
+    """The oracle loop with the PI controller (the reference integrator's
+    constants, beta 0.04) reaches tf on x' = x (the reference's exponential
+    problem) and on van der Pol with no more rejections than the elementary
+    controller, accurate to the tolerance's order; with beta = 0 and no
+    rejection it takes as many steps as the elementary controller."""
+    ode = orc.small_ode(orc.ODE_EXPONENTIAL, 10)
+    x0 = np.linspace(0.5, 1.5, 10)
+    tol = 1e-10
+    s = orc.Session("DOPRI5", ode, x0, 0.0, 1.0, tol, tol, controller="pi", pi_beta=0.04)
+    times, states = s.run()
+    st = s.stats()
+    s.close()
+    r = orc.integrate("DOPRI5", ode, x0, 0.0, 1.0, tol, tol)
+    assert times[-1] == 1.0
+    assert st["n_rejected"] <= r.stats["n_rejected"]
+    assert np.max(np.abs(states[-1] - np.e * x0) / (np.e * x0)) <= 1e3 * tol
+    s0 = orc.Session("DOPRI5", ode, x0, 0.0, 1.0, tol, tol, controller="pi", pi_beta=0.0)
+    t0s, _ = s0.run()
+    st0 = s0.stats()
+    s0.close()
+    if st0["n_rejected"] == 0 and r.stats["n_rejected"] == 0:
+        # the same formula (evaluated as safe * err^-alpha instead of
+        # safe / err^alpha): the same number of steps
+        assert abs(len(t0s) - len(r.times)) <= 1
+    vdp = orc.small_ode(orc.ODE_VANDERPOL, 2)
+    P = GOLD["problems"]["vanderpol"]
+    for tab in ("DOPRI5", "RKF78"):
+        sv = orc.Session(tab, vdp, np.array(P["x0"]), P["t0"], P["tf"], P["tol"], P["tol"],
+                         controller="pi")
+        tv, xv = sv.run()
+        stv = sv.stats()
+        sv.close()
+        rv = orc.integrate(tab, vdp, np.array(P["x0"]), P["t0"], P["tf"], P["tol"], P["tol"],
+                           capacity=1 << 16)
+        assert tv[-1] == P["tf"]
+        assert stv["n_rejected"] <= rv.stats["n_rejected"]
+        assert np.max(np.abs(xv[-1] - rv.states[-1])) <= 1e3 * P["tol"] * (1 + np.abs(xv[-1]).max())
+
+
+def test_dense_session_on_the_exponential(orc):
+    """Dense output from the oracle loop on x' = x (DOPRI5, tol 1e-10): the
+    continuous extension is accurate to the tolerance's order at times
+    between steps, and equals the step's own state at a step's end time."""
+    ode = orc.small_ode(orc.ODE_EXPONENTIAL, 10)
+    x0 = np.linspace(0.5, 1.5, 10)
+    ts = np.linspace(0.01, 0.99, 23)
+    s = orc.Session("DOPRI5", ode, x0, 0.0, 1.0, 1e-10, 1e-10, dense_times=ts)
+    times, states = s.run()
+    dense = s.dense()
+    s.close()
+    assert dense.shape == (len(ts), 10)
+    exact = np.exp(ts)[:, None] * x0[None, :]
+    assert np.max(np.abs(dense - exact) / exact) <= 1e-8
+    s2 = orc.Session("DOPRI5", ode, x0, 0.0, 1.0, 1e-10, 1e-10, dense_times=times[3:6])
+    s2.run()
+    np.testing.assert_allclose(s2.dense(), states[3:6], rtol=1e-15, atol=0)
+    s2.close()
