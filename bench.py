@@ -1,16 +1,23 @@
 """Benchmark of the GB300 adaptive embedded-RK N-body integrator.
 
-Workload (one GPU): one N = 16384 Plummer sphere (scale radius 1, velocities
-from the distribution function, seed 101), softening 0.005, the 13-stage
-Fehlberg 7(8) pair, atol = rtol = 1e-8, t in [0, 2], FP32 pair forces on
-hi/lo positions (hi/lo differences for close pairs) with Kahan-compensated
-accumulation, FP64 state / stage combination / norm.
-A step is one whole integration t = 0 -> 2 from the seeded state (about 150
-adaptive attempts): the initial-step estimate on the device, then attempts of
-13 fused stage kernels (force + next-stage combination) and one controller
-kernel, replayed 16 attempts per CUDA graph with the state resident in HBM.
+Workload (one GPU): the configuration-2 system -- one N = 16384 Plummer
+sphere (scale radius 1, velocities from the distribution function, seed 101),
+softening 0.005, the 13-stage Fehlberg 7(8) pair, t in [0, 2], FP32 pair
+forces on hi/lo positions with Kahan-compensated accumulation, FP64 state /
+stage combination / norm -- integrated at atol = rtol = 1e-11, the loosest
+tolerance measured at which its relative energy error over t = 0 -> 2 is at
+most 1e-8 (the metric's operating point; configuration 2's own 1e-8 gives
+~1e-7, reported beside it), with the learned step-size proposer trained at
+that tolerance (ode_prototyping_gb300/weights/).
+A step is one whole integration t = 0 -> 2 from the seeded state: the
+initial-step estimate on the device, then attempts of 13 fused stage kernels
+and one controller kernel, replayed 16 attempts per CUDA graph (each replay
+re-sorts the bodies along a Morton curve) with the state resident in HBM.
 value = accepted steps per second of device time (the host's polls between
-graph replays included).
+graph replays included); time_to_tf_s beside it.  The same line carries the
+plain FP64 GB300 path, the mixed path with the reference and PI controllers
+and the learned + mixed path, each over the whole trajectory at the same
+tolerance with its measured energy error.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -33,18 +40,27 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# configuration 2: the system, its tableau and time span (its tolerance 1e-8
+# is CONFIG2_TOL; the headline runs at METRIC_TOL)
+CONFIG2_TOL = 1e-8
+METRIC_TOL = 1e-11
+PROPOSER = "proposer_plummer16384_rkf78_tol1e-11.bin"
 WORKLOAD = {
-    "workload": "plummer16384_rkf78_mixed",
+    "workload": "plummer16384_rkf78_learned_mixed_tol1e-11",
     "n_particles": 16384,
     "model": "Plummer sphere a=1, G=1, equal masses 1/N",
     "seed": 101,
     "softening": 0.005,
     "tableau": "RKF78",
-    "atol": 1e-8,
-    "rtol": 1e-8,
+    "atol": METRIC_TOL,
+    "rtol": METRIC_TOL,
     "t0": 0.0,
     "tf": 2.0,
     "precision": "mixed",
+    "controller": "learned",
+    "proposer": PROPOSER,
+    "energy_target": "relative energy error over t0 -> tf <= 1e-8 (atol = rtol = 1e-11; "
+                     "configuration 2's tolerance 1e-8 gives ~1e-7)",
 }
 METRIC = "accepted steps/s and pair-interactions/s at equal energy error: learned+mixed vs FP64"
 FP32_LANES_PER_SM = 128
@@ -79,12 +95,13 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+        self.path = None
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.f = open(self.path, "w")
+            import tempfile
+            fd, self.path = tempfile.mkstemp(prefix=f"gbode_clocks_gpu{self.gpu}_", suffix=".csv")
+            self.f = os.fdopen(fd, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
                  "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
@@ -115,18 +132,20 @@ class ClockSampler:
             for name, v in zip(names, parts[5:9]):
                 if v.lower() in ("active", "1"):
                     reasons.add(name)
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def load_mlp(args):
-    if args.controller != "learned":
-        return None
+def load_mlp(path=None):
+    """Proposer weights (default: the one trained at the headline tolerance)."""
     import ode_prototyping_gb300 as gb
-    path = args.mlp or os.path.join(ROOT, "ode_prototyping_gb300", "weights",
-                                   "proposer_plummer16384_rkf78.bin")
+    path = path or os.path.join(ROOT, "ode_prototyping_gb300", "weights", PROPOSER)
     return gb.GbMlp.from_buffer_copy(open(path, "rb").read())
 
 
@@ -204,10 +223,9 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     import oracle
-    import ode_prototyping_gb300 as gb
     W = WORKLOAD
     n = W["n_particles"]
-    x0 = gb.ic_plummer(n, W["seed"], 1.0)
+    x0 = oracle.ic_plummer(n, W["seed"], 1.0)
     threads = os.cpu_count() or 1
     ode, _ = oracle.nbody_ode(n, W["softening"], 1.0 / n)
     sess = oracle.Session(W["tableau"], ode, x0, W["t0"], W["tf"], W["atol"], W["rtol"],
@@ -260,11 +278,10 @@ def cpu_baseline(attempts_per_accepted: float) -> dict:
     host clock.  Scaled to accepted steps/s with the trajectory's attempts per
     accepted step (the same algorithm, measured on the whole integration)."""
     import oracle
-    import ode_prototyping_gb300 as gb
     W = WORKLOAD
     n = W["n_particles"]
     threads = os.cpu_count() or 1
-    x0 = gb.ic_plummer(n, W["seed"], 1.0)
+    x0 = oracle.ic_plummer(n, W["seed"], 1.0)
     ode, _ = oracle.nbody_ode(n, W["softening"], 1.0 / n)
     sess = oracle.Session(W["tableau"], ode, x0, W["t0"], W["tf"], W["atol"], W["rtol"],
                           threads)
@@ -286,6 +303,94 @@ def cpu_baseline(attempts_per_accepted: float) -> dict:
             "pair_interactions_per_s": rhs * n * (n - 1) / t_att}
 
 
+def integrate_once(gb, torch, x0_dev, stream, precision: str, controller: str, tol: float,
+                   mlp=None):
+    """One whole integration t0 -> tf from x0 on `stream`: (device ms, stats,
+    final state).  The integrator is created outside the timed region."""
+    W = WORKLOAD
+    n = W["n_particles"]
+    exe = gb.Gb300Executor(precision=precision, controller=controller, attempts_per_sync=16,
+                           mlp=mlp if controller == "learned" else None)
+    it = gb.Integrator(W["tableau"], gb.NBodyODE(n, W["softening"], 1.0 / n), exe,
+                       stream=stream)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        it.start(x0_dev, W["t0"], W["tf"], tol, tol)
+        rc = it.advance(0)
+        b.record(stream)
+    stream.synchronize()
+    if rc != 0:
+        raise RuntimeError(f"{precision}/{controller} integration failed with status {rc}")
+    st = it.stats()
+    xs, _ = it.state()
+    xs = xs.clone()
+    it.close()
+    return a.elapsed_time(b), st, xs
+
+
+def arm_record(gb, x0_dev, e0, ms, st, xs) -> dict:
+    W = WORKLOAD
+    n = W["n_particles"]
+    e1 = gb.energy(xs, n, W["softening"], 1.0 / n)
+    return {"time_to_tf_s": ms / 1e3, "accepted_steps_per_s": st["n_accepted"] / (ms / 1e3),
+            "accepted": st["n_accepted"], "attempts": st["n_attempts"],
+            "rejected_fraction": 1 - st["n_accepted"] / max(st["n_attempts"], 1),
+            "rhs_evals": st["n_rhs"], "t_reached": st["t"],
+            "pair_interactions_per_s": st["n_rhs"] * n * (n - 1) / (ms / 1e3), **drift(e0, e1)}
+
+
+def metric_arms(gb, torch, x0_dev, e0, headline: dict, mlp) -> dict:
+    """The metric: learned + mixed against the plain FP64 GB300 path at equal
+    relative energy error <= 1e-8, every arm over the whole trajectory t0 ->
+    tf at the same tolerance (the headline's): FP64 with the reference
+    controller, mixed with the reference and PI controllers, learned + mixed
+    (the headline's own last step).  Speed-ups are ratios of time to tf; the
+    accepted-steps/s ratios sit beside them."""
+    stream = torch.cuda.Stream()
+    out = {"tol": METRIC_TOL, "learned_mixed": headline}
+    for key, prec, ctl in (("mixed_reference", "mixed", "reference"), ("mixed_pi", "mixed", "pi"),
+                           ("f64_reference", "f64", "reference")):
+        ms, st, xs = integrate_once(gb, torch, x0_dev, stream, prec, ctl, METRIC_TOL)
+        out[key] = arm_record(gb, x0_dev, e0, ms, st, xs)
+    f64 = out["f64_reference"]
+    for key in ("learned_mixed", "mixed_reference", "mixed_pi"):
+        out[f"speedup_time_to_tf_{key}_vs_f64"] = f64["time_to_tf_s"] / out[key]["time_to_tf_s"]
+        out[f"speedup_accepted_steps_per_s_{key}_vs_f64"] = (
+            out[key]["accepted_steps_per_s"] / f64["accepted_steps_per_s"])
+    out["energy_errors_le_1e-8"] = all(out[k]["energy_rel_err"] <= 1e-8 for k in
+                                       ("learned_mixed", "mixed_reference", "mixed_pi",
+                                        "f64_reference"))
+    out["rhs_saved_learned_vs_reference"] = 1 - headline["rhs_evals"] / max(
+        out["mixed_reference"]["rhs_evals"], 1)
+    out["rhs_saved_learned_vs_pi"] = 1 - headline["rhs_evals"] / max(
+        out["mixed_pi"]["rhs_evals"], 1)
+    return out
+
+
+def config2_tolerance(gb, torch, x0_dev, e0) -> dict:
+    """Configuration 2 at its own tolerance (1e-8): the mixed path with the
+    reference controller, whole trajectory (energy error ~1e-7)."""
+    stream = torch.cuda.Stream()
+    integrate_once(gb, torch, x0_dev, stream, "mixed", "reference", CONFIG2_TOL)  # warm-up
+    ms, st, xs = integrate_once(gb, torch, x0_dev, stream, "mixed", "reference", CONFIG2_TOL)
+    return {"tol": CONFIG2_TOL, "controller": "reference", "precision": "mixed",
+            **arm_record(gb, x0_dev, e0, ms, st, xs)}
+
+
+def mixed_accuracy(gb, x0, n: int, eps: float) -> dict:
+    """Accelerations of the mixed path against FP64 on the initial state:
+    normwise and per-body relative error (median, 99.9th percentile, max)."""
+    ref = gb.nbody_rhs_f64(x0, n, eps, 1.0 / n).cpu().numpy()[3 * n:].reshape(-1, 3)
+    got = gb.nbody_rhs_mixed(x0, n, eps, 1.0 / n).cpu().numpy()[3 * n:].reshape(-1, 3)
+    per = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    return {"normwise": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+            "per_body_median": float(np.median(per)),
+            "per_body_p999": float(np.quantile(per, 0.999)), "per_body_max": float(per.max()),
+            "bodies_above_1e-6": int((per > 1e-6).sum()), "bodies": n}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -293,9 +398,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--controller", default="reference", choices=["reference", "pi", "learned"])
-    ap.add_argument("--mlp", default=None, help="trained proposer weights (learned controller)")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the comparison arms (FP64, mixed reference / PI)")
+    ap.add_argument("--mlp", default=None, help="proposer weights for the learned controller")
     ap.add_argument("--n-bodies", type=int, default=16384, help="stage: bodies")
     ap.add_argument("--stage-precision", default="mixed", choices=["mixed", "f64"],
                     help="stage: precision of the integrator")
@@ -329,8 +434,9 @@ def main():
     stream = torch.cuda.Stream()
     ode = gb.NBodyODE(n, eps, 1.0 / n)
     A = 16
-    exe = gb.Gb300Executor(precision=W["precision"], controller=args.controller,
-                           attempts_per_sync=A, mlp=load_mlp(args))
+    mlp = load_mlp(args.mlp)
+    exe = gb.Gb300Executor(precision=W["precision"], controller=W["controller"],
+                           attempts_per_sync=A, mlp=mlp)
     S = gb.tableau(W["tableau"]).n_stages
     it = gb.Integrator(W["tableau"], ode, exe, stream=stream)
     x0_dev = gb.to_device(x0)
@@ -372,52 +478,66 @@ def main():
     xs, t_now = it.state()
     e1 = gb.energy(xs, n, eps, 1.0 / n)
     cons = drift(e0, e1)
-    energy_err = cons["energy_rel_err"]
     per_job = {"accepted": accepted // max(args.steps, 1), "attempts": attempts // max(args.steps, 1),
                "rhs_evals": rhs // max(args.steps, 1)}
-    # launches per job: start-up kernels + graph replays of A attempts x (S + 1)
+    # launches per job: start-up kernels (initial step, packing, first sort)
+    # + per graph replay the re-sort (3 kernels of this library, the radix
+    # sort's own kernels not counted) and A x (S stage kernels + 1 controller)
     replays = -(-per_job["attempts"] // A)
-    launches_per_job = 12 + replays * A * (S + 1)
+    launches_per_job = 15 + replays * (3 + A * (S + 1))
     # whole-job aggregate over ranks: accepted steps summed, time = max
     acc_all, rhs_all, ms_max = aggregate_over_ranks(float(accepted), float(rhs), ms)
     value = acc_all / (ms_max / 1e3)
     pair_rate = rhs_all * n * (n - 1) / (ms_max / 1e3)
+    headline = {"time_to_tf_s": ms / 1e3 / max(args.steps, 1),
+                "accepted_steps_per_s": accepted / (ms / 1e3), "accepted": per_job["accepted"],
+                "attempts": per_job["attempts"],
+                "rejected_fraction": 1 - accepted / max(attempts, 1),
+                "rhs_evals": per_job["rhs_evals"], "t_reached": t_now,
+                "pair_interactions_per_s": rhs * n * (n - 1) / (ms / 1e3), **cons}
 
-    # dominant kernel: the fused stage kernel, timed alone on its stream on a
-    # live integrator (restarted, so no launch finds the integration finished)
+    # dominant kernel: the fused stage kernel on a live integrator
+    # (restarted, so no launch finds the integration finished), timed as
+    # launched inside an attempt: 11 stage launches back to back after an
+    # L2 flush, CUDA events around the run (on the integrator's stream),
+    # repeated 10 times; kernel_ms = the mean per launch
     it.start(x0_dev, W["t0"], W["tf"], W["atol"], W["rtol"])
     geo = it.geometry()
-    reps = 20
+    reps = 10
     ks0 = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
     ks1 = [torch.cuda.Event(enable_timing=True) for _ in range(reps)]
     with torch.cuda.stream(stream):
         for r in range(reps):
             flush.fill_(r & 0xFF)
             ks0[r].record(stream)
-            it.launch_stage(1 + r % (S - 2))
+            for s in range(1, S - 1):
+                it.launch_stage(s)
             ks1[r].record(stream)
     stream.synchronize()
-    k_ms = statistics.mean(a.elapsed_time(b) for a, b in zip(ks0, ks1))
+    k_ms = statistics.mean(a.elapsed_time(b) for a, b in zip(ks0, ks1)) / (S - 2)
     achieved = FLOPS_PER_INTERACTION * n * (n - 1) / (k_ms / 1e3) / 1e12
     pk, pk_kind = peaks()
     sm_mhz_max = float(pk.get("sm_max_mhz", 2070.0))
     n_sm = torch.cuda.get_device_properties(local).multi_processor_count
     fp32_peak = n_sm * FP32_LANES_PER_SM * 2 * sm_mhz_max * 1e6 / 1e12
     it.close()
+    stage_launches = per_job["rhs_evals"] - 2  # minus the initial step's two RHS
 
     line = {
         "metric": METRIC, "value": value, "unit": "accepted steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic",
-        "config": {**W, "controller": args.controller, "parallelism": f"replicas{world}",
+        "config": {**W, "parallelism": f"replicas{world}",
                    "l2": "flushed between timed steps (256 MiB write)",
                    "step": "one whole integration t0 -> tf from the seeded state: initial "
                            "step on the device, then attempts of 13 fused stage kernels + "
-                           "1 controller kernel replayed 16 per CUDA graph"},
+                           "1 controller kernel replayed 16 per CUDA graph, bodies re-sorted "
+                           "along a Morton curve at every replay"},
+        "time_to_tf_s": headline["time_to_tf_s"],
         "pair_interactions_per_s": pair_rate,
-        "per_step": per_job, "rejected_fraction": 1 - accepted / max(attempts, 1),
-        "t_reached": t_now, "energy_rel_err": energy_err,
+        "per_step": per_job, "rejected_fraction": headline["rejected_fraction"],
+        "t_reached": t_now, "energy_rel_err": cons["energy_rel_err"],
         "momentum_drift": cons["momentum_drift"],
         "angular_momentum_drift": cons["angular_momentum_drift"],
         "clocks": clocks,
@@ -430,6 +550,10 @@ def main():
                                      "served from L2)",
                      "kernel": stage_kernel_name(W["precision"], geo),
                      "kernel_ms": k_ms, "geometry": geo,
+                     "kernel_timing": "mean per launch over 10 runs of 11 back-to-back stage "
+                                      "launches (L2 flushed before each run), CUDA events on "
+                                      "the launching stream",
+                     "stage_launches_per_step_x_kernel_ms": stage_launches * k_ms,
                      "peak_note": f"nominal FP32 pipe: {n_sm} SMs x {FP32_LANES_PER_SM} lanes x 2"
                                   f" x {sm_mhz_max:.0f} MHz ({pk_kind} peaks file has no FP32)",
                      "flops_per_interaction": FLOPS_PER_INTERACTION,
@@ -437,13 +561,16 @@ def main():
                      "fp32_pipe_cap_frac": FLOPS_PER_INTERACTION / 2 / HILO_FP32_OPS},
     }
     if rank == 0:
-        line["e2e"] = e2e(gb, torch, x0)
+        line["e2e"] = e2e(gb, torch, x0, mlp)
+        line["mixed_accuracy"] = mixed_accuracy(gb, x0_dev, n, eps)
+        line["config2_tol_1e-8"] = config2_tolerance(gb, torch, x0_dev, e0)
         if not args.no_fp64:
-            line["fp64_comparison"] = fp64_compare(gb, torch, x0, line)
-            line["equal_energy_le_1e-8"] = energy_target_compare(gb, torch, x0)
+            line["equal_energy_le_1e-8"] = metric_arms(gb, torch, x0_dev, e0, headline, mlp)
         if not args.no_cpu_baseline:
             try:
-                line["cpu_baseline"] = cpu_baseline(attempts / max(accepted, 1))
+                apa = line.get("equal_energy_le_1e-8", {}).get("mixed_reference", {})
+                ratio = apa.get("attempts", 552) / max(apa.get("accepted", 463), 1)
+                line["cpu_baseline"] = cpu_baseline(ratio)
             except Exception as ex:  # reported, not fatal
                 line["cpu_baseline"] = {"value": None, "error": repr(ex)}
         print(json.dumps(line), flush=True)
@@ -578,49 +705,91 @@ def run_other_workload(args):
                             "step": "whole integration"})
         it.close()
     elif args.workload in ("c3", "c5b"):
+        # Batched ensembles, every arm over the whole [0, tf] of every system:
+        # mixed with the reference controller, mixed with the learned
+        # proposer (PI fallback), and the plain FP64 path; per-system relative
+        # energy errors at tf (max and median) beside the throughput.
         if args.workload == "c3":
+            # configuration 3: 512 Plummer spheres, N log-uniform in [64, 4096],
+            # virial ratio U(0.5, 1.5), eps = 0.01 * 4 / N^(1/3), DOPRI5, tol 1e-9
             rng = np.random.default_rng(303)
             sizes = np.round(np.exp(rng.uniform(np.log(64), np.log(4096), 512))).astype(np.int64)
             eps = 0.01 * 4.0 / np.cbrt(sizes)
             x0 = _batch_ics(gb, torch, sizes, 3000 + np.arange(512), "virial", eps)
             tab, tol, tf = "DOPRI5", 1e-9, 1.0
+            prop = "proposer_batch_dopri5_tol1e-9.bin"
         else:
+            # configuration 5, batched part: 64 binary-rich Plummer spheres of
+            # N = 8192 (10 % of the bodies in bound pairs, semimajor axes
+            # log-uniform in [1e-3, 1e-2]); the configuration gives no
+            # softening, the pairs need one well below their separations:
+            # eps = 1e-4; DOPRI5, tol 1e-8, t in [0, 5e-4] (the FP64 arm takes
+            # about two minutes over it)
             sizes = np.full(64, 8192, dtype=np.int64)
             eps = np.full(64, 1e-4)
             x0 = _batch_ics(gb, torch, sizes, 6000 + np.arange(64), "binary", eps)
-            tab, tol, tf = "DOPRI5", 1e-8, 0.002
+            tab, tol, tf = "DOPRI5", 1e-8, 5e-4
+            prop = "proposer_binary2048_dopri5.bin"
         x0d = gb.to_device(x0)
+        offs = np.concatenate([[0], np.cumsum(sizes)]) * 6
+        e0 = [gb.energy(x0d[offs[k]:offs[k + 1]], int(sizes[k]), float(eps[k]), 1.0 / sizes[k])
+              for k in range(len(sizes))]
+        ppath = os.path.join(ROOT, "ode_prototyping_gb300", "weights", prop)
+        mlp = (gb.GbMlp.from_buffer_copy(open(ppath, "rb").read())
+               if os.path.exists(ppath) else None)
         res = {}
-        for prec in ("mixed", "f64"):
-            b = gb.Batch(tab, sizes, eps, precision=prec, attempts_per_sync=8, stream=stream)
+        arms = [("mixed", "mixed", "reference"), ("f64", "f64", "reference")]
+        if mlp is not None:
+            arms.insert(1, ("learned_mixed", "mixed", "learned"))
+        for key, prec, ctl in arms:
+            b = gb.Batch(tab, sizes, eps, precision=prec, controller=ctl, attempts_per_sync=8,
+                         stream=stream, mlp=mlp if ctl == "learned" else None)
             b.start(x0d, 0.0, tf, tol, tol)
             tune = b.autotune(2)
-            limit = 0 if prec == "mixed" else 3  # FP64: a bounded window of graph replays
 
             def job():
                 b.start(x0d, 0.0, tf, tol, tol)
-                b.advance(limit)
+                rc = b.advance(0)
+                assert rc == 0, rc
                 return b.stats()
+            reps = args.steps if prec == "mixed" else 1
             if prec == "mixed":
                 for _ in range(args.warmup):
                     job()
-            ms, st = _timed(torch, stream, job, args.steps if prec == "mixed" else 1, flush)
+            ms, st = _timed(torch, stream, job, reps, flush)
+            xs, ts = b.state()
+            errs = []
+            for k in range(len(sizes)):
+                e1 = gb.energy(xs[offs[k]:offs[k + 1]], int(sizes[k]), float(eps[k]),
+                               1.0 / sizes[k])
+                errs.append(abs(e1["e"] - e0[k]["e"]) / abs(e0[k]["e"]))
             acc = sum(s["n_accepted"] for s in st)
             inter = sum(s["interactions"] for s in st)
-            res[prec] = {"accepted_steps_per_s": acc / (ms / 1e3),
-                         "pair_interactions_per_s": inter / (ms / 1e3),
-                         "ms_per_step": ms / len(st), "geometry": tune,
-                         "accepted": st[0]["n_accepted"], "attempts": st[0]["n_attempts"],
-                         "t_min": st[0]["t"], "done": st[0]["done"]}
+            res[key] = {"accepted_steps_per_s": acc / (ms / 1e3),
+                        "pair_interactions_per_s": inter / (ms / 1e3),
+                        "time_to_tf_s": ms / len(st) / 1e3, "geometry": tune,
+                        "accepted": st[0]["n_accepted"], "attempts": st[0]["n_attempts"],
+                        "rhs_evals": st[0]["n_rhs"], "t_min": float(ts.min()),
+                        "energy_rel_err_max": float(np.max(errs)),
+                        "energy_rel_err_median": float(np.median(errs))}
             b.close()
-        line.update(value=res["mixed"]["accepted_steps_per_s"], dtype="f32+f64",
-                    steps=args.steps, ms_per_step=res["mixed"]["ms_per_step"],
-                    pair_interactions_per_s=res["mixed"]["pair_interactions_per_s"],
-                    fp64_comparison=res,
+        f64 = res["f64"]
+        for key in res:
+            if key != "f64":
+                res[f"speedup_time_to_tf_{key}_vs_f64"] = (f64["time_to_tf_s"]
+                                                           / res[key]["time_to_tf_s"])
+        head = res["learned_mixed"] if "learned_mixed" in res else res["mixed"]
+        line.update(value=head["accepted_steps_per_s"], dtype="f32+f64",
+                    steps=args.steps, ms_per_step=1e3 * head["time_to_tf_s"],
+                    pair_interactions_per_s=head["pair_interactions_per_s"], arms=res,
                     config={"workload": args.workload, "systems": int(len(sizes)),
                             "n_min": int(sizes.min()), "n_max": int(sizes.max()),
                             "bodies": int(sizes.sum()), "tableau": tab, "atol": tol,
-                            "rtol": tol, "t": [0, tf], "step": "whole batch integration"})
+                            "rtol": tol, "t": [0, tf],
+                            "softening": "0.01 * 4 / N^(1/3)" if args.workload == "c3"
+                            else float(eps[0]),
+                            "proposer": prop if mlp is not None else None,
+                            "step": "whole batch integration, every system to tf"})
     elif args.workload == "stage":
         # Four stage launches of the headline integrator on an N-body Plummer
         # sphere (a small case for profiling the fused stage kernel).
@@ -735,8 +904,16 @@ def run_other_workload(args):
                     config={"workload": "rkf78_elementwise_nvar16777216", "n_var": nv,
                             "tableau": "RKF78", "l2": "flushed (256 MiB write) before each call"})
     else:  # c5a
+        # Configuration 5, single system: N = 262144 cold collapse (uniform
+        # sphere, velocities 1 % Gaussian noise, eps = 0.002), DOPRI5, tol
+        # 1e-8.  The mixed path runs `steps` timed attempts after the warm-up
+        # ones; then every arm integrates the same window [0, t_w] (t_w =
+        # where those attempts ended) from the initial state: mixed with the
+        # reference controller, mixed with the learned proposer, and the plain
+        # FP64 path, each with its time and relative energy error at t_w.
         n, eps, tol = 262144, 0.002, 1e-8
         x0 = gb.to_device(gb.ic_cold_sphere(n, 505, 0.01))
+        e0 = gb.energy(x0, n, eps, 1.0 / n)
         it = gb.Integrator("DOPRI5", gb.NBodyODE(n, eps, 1.0 / n),
                            gb.Gb300Executor(precision="mixed", attempts_per_sync=1),
                            stream=stream)
@@ -749,26 +926,57 @@ def run_other_workload(args):
         s1 = it.stats()
         acc = s1["n_accepted"] - s0["n_accepted"]
         rhs = s1["n_rhs"] - s0["n_rhs"]
-        xs, t = it.state()
+        xs, t_w = it.state()
         it.close()
         # accelerations of the mixed path against FP64 on the current state
-        f64 = gb.nbody_rhs_f64(xs, n, eps, 1.0 / n)
+        f64 = gb.nbody_rhs_f64(xs, n, eps, 1.0 / n, tile=gb.tiling(f64_pair=1))
         mx = gb.nbody_rhs_mixed(xs, n, eps, 1.0 / n)
         a64, amx = f64[3 * n:].view(-1, 3), mx[3 * n:].view(-1, 3)
         rel = ((amx - a64).norm() / a64.norm()).item()
-        per = ((amx - a64).norm(dim=1) / a64.norm(dim=1)).median().item()
+        per_b = ((amx - a64).norm(dim=1) / a64.norm(dim=1))
+        window = {"t_w": t_w}
+        ppath = os.path.join(ROOT, "ode_prototyping_gb300", "weights",
+                             "proposer_binary2048_dopri5.bin")
+        mlp = gb.GbMlp.from_buffer_copy(open(ppath, "rb").read())
+        for key, prec, ctl in (("mixed", "mixed", "reference"),
+                               ("learned_mixed", "mixed", "learned"),
+                               ("f64", "f64", "reference")):
+            itw = gb.Integrator("DOPRI5", gb.NBodyODE(n, eps, 1.0 / n),
+                                gb.Gb300Executor(precision=prec, controller=ctl,
+                                                 attempts_per_sync=4,
+                                                 mlp=mlp if ctl == "learned" else None),
+                                stream=stream)
+
+            def job():
+                itw.start(x0, 0.0, t_w, tol, tol)
+                assert itw.advance(0) == 0
+                return itw.stats()
+            wms, wst = _timed(torch, stream, job, 1, flush)
+            e1 = gb.energy(itw.state()[0], n, eps, 1.0 / n)
+            window[key] = {"time_to_t_w_s": wms / 1e3, "accepted": wst[0]["n_accepted"],
+                           "attempts": wst[0]["n_attempts"], "rhs_evals": wst[0]["n_rhs"],
+                           "accepted_steps_per_s": wst[0]["n_accepted"] / (wms / 1e3),
+                           **drift(e0, e1)}
+            itw.close()
+        for key in ("mixed", "learned_mixed"):
+            window[f"speedup_time_{key}_vs_f64"] = (window["f64"]["time_to_t_w_s"]
+                                                    / window[key]["time_to_t_w_s"])
         line.update(value=acc / (ms / 1e3), dtype="f32+f64", steps=args.steps,
                     ms_per_step=ms / args.steps,
                     pair_interactions_per_s=rhs * n * (n - 1) / (ms / 1e3),
-                    accepted=acc, t_reached=t, acc_rel_err_normwise=rel,
-                    acc_rel_err_median=per,
+                    accepted=acc, t_reached=t_w, acc_rel_err_normwise=rel,
+                    acc_rel_err_median=per_b.median().item(),
+                    acc_rel_err_p999=per_b.quantile(0.999).item(),
+                    acc_rel_err_max=per_b.max().item(), window=window,
                     config={"workload": "cold_collapse262144_dopri5_mixed", "n_particles": n,
                             "softening": eps, "tableau": "DOPRI5", "atol": tol, "rtol": tol,
+                            "proposer": "proposer_binary2048_dopri5.bin (DOPRI5, trained on "
+                                        "binary-rich N = 2048 systems, not on this one)",
                             "step": "one adaptive attempt"})
     print(json.dumps(line), flush=True)
 
 
-def e2e(gb, torch, x0: np.ndarray, reps: int = 3) -> dict:
+def e2e(gb, torch, x0: np.ndarray, mlp, reps: int = 3) -> dict:
     """Same metric through the public API from host memory: pinned host state
     -> device, integrator creation + initial step + the whole integration,
     final state -> host; host clock around everything.  Each of `reps` runs
@@ -782,7 +990,8 @@ def e2e(gb, torch, x0: np.ndarray, reps: int = 3) -> dict:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         dev = host.to("cuda", non_blocking=True)
-        exe = gb.Gb300Executor(precision=W["precision"], attempts_per_sync=16)
+        exe = gb.Gb300Executor(precision=W["precision"], controller=W["controller"],
+                               attempts_per_sync=16, mlp=mlp)
         it = gb.Integrator(W["tableau"], gb.NBodyODE(n, W["softening"], 1.0 / n), exe)
         it.start(dev, W["t0"], W["tf"], W["atol"], W["rtol"])
         it.advance(0)
@@ -799,109 +1008,6 @@ def e2e(gb, torch, x0: np.ndarray, reps: int = 3) -> dict:
             "note": "per run: one whole integration through the public API; creation, "
                     "initial-step estimate and graph build inside the timed region; "
                     "value = median of the runs"}
-
-
-def fp64_compare(gb, torch, x0, line, k: int = 6) -> dict:
-    """The plain FP64 GB300 path on the same workload, same tolerance, for k
-    attempts (its throughput), and the mixed path over the same k attempts
-    (energy error over the same interval)."""
-    W = WORKLOAD
-    n = W["n_particles"]
-    res = {}
-    for prec in ("f64", "mixed"):
-        stream = torch.cuda.Stream()
-        exe = gb.Gb300Executor(precision=prec, attempts_per_sync=1)
-        it = gb.Integrator(W["tableau"], gb.NBodyODE(n, W["softening"], 1.0 / n), exe,
-                           stream=stream)
-        it.start(x0, W["t0"], W["tf"], W["atol"], W["rtol"])
-        it.sync()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        s0 = it.stats()
-        a.record(stream)
-        it.enqueue(k)
-        b.record(stream)
-        stream.synchronize()
-        it.sync()
-        s1 = it.stats()
-        xs, t = it.state()
-        e0 = gb.energy(x0, n, W["softening"], 1.0 / n)
-        e1 = gb.energy(xs, n, W["softening"], 1.0 / n)
-        ms = a.elapsed_time(b)
-        res[prec] = {"accepted_steps_per_s": (s1["n_accepted"] - s0["n_accepted"]) / (ms / 1e3),
-                     "attempts": k, "t_reached": t,
-                     **drift(e0, e1), "ms": ms}
-        res[prec + "_state"] = xs
-        it.close()
-    diff = (res["mixed_state"] - res["f64_state"]).abs().max().item()
-    del res["mixed_state"], res["f64_state"]
-    res["max_state_diff_mixed_vs_f64"] = diff
-    res["speedup_mixed_vs_f64"] = (res["mixed"]["accepted_steps_per_s"] /
-                                   max(res["f64"]["accepted_steps_per_s"], 1e-30))
-    return res
-
-
-def energy_target_compare(gb, torch, x0, tol: float = 1e-11, skip: int = 4,
-                          k: int = 8) -> dict:
-    """The same system at a tolerance where the relative energy error over
-    t0 -> tf is at most 1e-8: the mixed path's whole trajectory with the
-    reference controller and with the learned proposer trained at this
-    tolerance (energy errors measured), and the plain FP64 path's throughput
-    over k attempts at the same tolerance after `skip` untimed start-up
-    attempts (the FP64 whole trajectory takes minutes: python bench.py
-    --workload c2_tol --tol 1e-11)."""
-    W = WORKLOAD
-    n = W["n_particles"]
-    stream = torch.cuda.Stream()
-    out = {"tol": tol}
-    # the proposer trained at this tolerance (ode_prototyping_gb300/learned.py)
-    mlp = gb.GbMlp.from_buffer_copy(open(os.path.join(
-        ROOT, "ode_prototyping_gb300", "weights", "proposer_plummer16384_rkf78_tol1e-11.bin"),
-        "rb").read())
-    for key in ("mixed", "mixed_learned", "f64"):
-        prec = "f64" if key == "f64" else "mixed"
-        learned = key == "mixed_learned"
-        exe = gb.Gb300Executor(precision=prec, attempts_per_sync=16 if prec == "mixed" else 1,
-                               controller="learned" if learned else "reference",
-                               mlp=mlp if learned else None)
-        it = gb.Integrator(W["tableau"], gb.NBodyODE(n, W["softening"], 1.0 / n), exe,
-                           stream=stream)
-        it.start(x0, W["t0"], W["tf"], tol, tol)
-        it.sync()
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        if prec == "f64":
-            it.enqueue(skip)
-            it.sync()
-        s0 = it.stats()
-        a.record(stream)
-        if prec == "mixed":
-            it.advance(0)
-        else:
-            it.enqueue(k)
-        b.record(stream)
-        stream.synchronize()
-        it.sync()
-        s1 = it.stats()
-        xs, t = it.state()
-        ms = a.elapsed_time(b)
-        r = {"accepted_steps_per_s": (s1["n_accepted"] - s0["n_accepted"]) / (ms / 1e3),
-             "accepted": s1["n_accepted"] - s0["n_accepted"],
-             "attempts": s1["n_attempts"] - s0["n_attempts"],
-             "rhs_evals": s1["n_rhs"] - s0["n_rhs"], "t_reached": t, "ms": ms}
-        if prec == "mixed":
-            e0 = gb.energy(x0, n, W["softening"], 1.0 / n)
-            r.update(drift(e0, gb.energy(xs, n, W["softening"], 1.0 / n)))
-        else:
-            r["window"] = f"{k} attempts after {skip} start-up attempts"
-        out[key] = r
-        it.close()
-    f64 = max(out["f64"]["accepted_steps_per_s"], 1e-30)
-    out["speedup_mixed_vs_f64"] = out["mixed"]["accepted_steps_per_s"] / f64
-    out["speedup_mixed_learned_vs_f64"] = out["mixed_learned"]["accepted_steps_per_s"] / f64
-    out["rhs_saved_learned_vs_reference"] = (1.0 - out["mixed_learned"]["rhs_evals"] /
-                                            max(out["mixed"]["rhs_evals"], 1))
-    return out
 
 
 if __name__ == "__main__":

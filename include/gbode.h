@@ -115,6 +115,12 @@ typedef struct {
                             partners with two bodies per thread, 3 = the same with one
                             body per thread; the packed loops need uniform masses
                             (per-body masses run the scalar loop) */
+  int32_t f64_pair;      /* FP64 pair term: 0 = the entry point's default, 1 = r^-3 from a
+                            Newton-refined reciprocal square root with fused multiply-add
+                            sums (a few ulp per term, ~2.5x fewer FP64 operations), 2 = the
+                            reference's operation order (IEEE sqrt and divisions,
+                            NBodyODE.hpp:89-98).  The standalone right-hand sides default to
+                            2; the integrator's FP64 stages default to 1 (exact mode: 2) */
 } gb_force_tiling;
 
 int gb_nbody_rhs_f64(const double* x_dev, double* dxdt_dev, int64_t n_particles,
@@ -304,8 +310,13 @@ typedef struct {
   gb_force_tiling tiling;     /* 0 fields = auto */
   const void* mlp;            /* gb_mlp* weights for GB_CTRL_LEARNED (device-resident copy made) */
   int32_t log_steps;          /* record per-attempt controller logs on the device */
-  int32_t spatial_sort;       /* mixed precision: 1 = Morton-sorted tiles with the
-                                 far-field path (pays off for large N), 0 = off */
+  int32_t spatial_sort;       /* mixed precision: 0 = default (uniform masses, N >= 8192:
+                                 the partner-chunk stage on Morton-sorted bodies, where
+                                 half tiles whose boxes are far from the i-tile skip the
+                                 close-pair test), 1 = Morton-sorted tiles with the
+                                 tile-centroid far-field path, 2 = the sorted chunk stage
+                                 without that culling (the same bits as 0), 3 = the
+                                 chunk stage in body order */
 } gb_integrate_opts;
 
 typedef struct {

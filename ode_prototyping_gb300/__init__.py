@@ -50,7 +50,7 @@ class GbTableau(C.Structure):
 
 class GbForceTiling(C.Structure):
     _fields_ = [("j_split", C.c_int32), ("lanes", C.c_int32), ("bodies_per_cta", C.c_int32),
-                ("mixed_variant", C.c_int32)]
+                ("mixed_variant", C.c_int32), ("f64_pair", C.c_int32)]
 
 
 class GbNBodySystem(C.Structure):
@@ -261,12 +261,13 @@ def tableau(name_or_struct) -> GbTableau:
 
 
 def tiling(j_split=0, lanes=0, bodies_per_cta=0, scalar=False,
-           mixed_variant=0) -> GbForceTiling:
+           mixed_variant=0, f64_pair=0) -> GbForceTiling:
     """Force-kernel tiling.  Mixed precision: scalar=True (or mixed_variant=1)
     selects the scalar FP32 pair loop, mixed_variant=2 / 3 the packed f32x2
     loop over pairs of partners with two bodies / one body per thread, 0 the
-    library's choice (3)."""
-    return GbForceTiling(j_split, lanes, bodies_per_cta, 1 if scalar else mixed_variant)
+    library's choice (3).  FP64: f64_pair=1 the refined-rsqrt pair term,
+    2 the reference's operation order, 0 the entry point's default."""
+    return GbForceTiling(j_split, lanes, bodies_per_cta, 1 if scalar else mixed_variant, f64_pair)
 
 
 # ----------------------------------------------------------------------------
@@ -466,7 +467,11 @@ class Gb300Executor:
     pi_beta: float = 0.04
     mlp: GbMlp | None = None
     log_steps: int = 0
-    spatial_sort: bool = False
+    # mixed precision: 0 = default (from N = 8192 the partner-chunk stage on
+    # Morton-sorted bodies with tile culling), 1 = the tile-centroid far-field
+    # path, 2 = the sorted chunk stage without culling (same bits as 0),
+    # 3 = the chunk stage in body order
+    spatial_sort: int = 0
     host_wait_timeout_s: float = 600.0  # bound on each host wait for the device
 
     def rhs(self, ode: NBodyODE, x, dxdt):
@@ -494,7 +499,7 @@ class Gb300Executor:
             self._mlp_keep = self.mlp
             o.mlp = C.cast(C.pointer(self.mlp), C.c_void_p)
         o.log_steps = self.log_steps
-        o.spatial_sort = 1 if self.spatial_sort else 0
+        o.spatial_sort = int(self.spatial_sort)
         return o
 
 

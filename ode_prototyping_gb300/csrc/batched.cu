@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(T)
     if (!skip_force) {
       if constexpr (PREC == GB_PREC_F64) {
         double* sh_pos = reinterpret_cast<double*>(sh_raw);
-        force_f64_cta<T, L>(ysrc, n, i0, 0, n, sy.eps2, nullptr, sh_pos, sh_pos + 3 * T, part);
+        force_f64_cta<T, L>(ysrc, n, i0, 0, n, sy.eps2, nullptr, sh_pos, sh_pos + 3 * T, part,
+                            true);
       } else {
         const PackedBody* src = (s == 0) ? P.PX + (long long)px * P.total_bodies + sy.body_off
                                          : P.PY + (long long)(s & 1) * P.total_bodies + sy.body_off;

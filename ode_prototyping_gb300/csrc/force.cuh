@@ -118,12 +118,17 @@ __device__ __forceinline__ void cluster_combine_rows(double (*part)[3], int rank
 // ---------------------------------------------------------------------------
 // FP64: partial sums of one CTA over its partner chunk.  sh_pos holds 3*T
 // doubles, sh_m T doubles (per-body masses only).  Results land in part[b].
+// fast = false: every pair term in the reference's operation order (IEEE
+// sqrt and divisions, NBodyODE.hpp:89-98), summed with IEEE adds; fast =
+// true: r^-3 from the refined reciprocal square root (rinv3_f64) and fused
+// multiply-add accumulation, a few ulp per term from the reference's.
 // ---------------------------------------------------------------------------
 template <int T, int L>
 __device__ __forceinline__ void force_f64_cta(const double* __restrict__ pos, long long n,
                                               long long i0, long long jb, long long je,
                                               double eps2, const double* __restrict__ masses,
-                                              double* sh_pos, double* sh_m, double (*part)[3]) {
+                                              double* sh_pos, double* sh_m, double (*part)[3],
+                                              bool fast = false) {
   constexpr int BI = T / L;
   const int b = threadIdx.x / L;
   const int l = threadIdx.x % L;
@@ -142,7 +147,20 @@ __device__ __forceinline__ void force_f64_cta(const double* __restrict__ pos, lo
     if (masses)
       for (int k = threadIdx.x; k < cnt; k += T) sh_m[k] = masses[j0 + k];
     __syncthreads();
-    if (i < n) {
+    if (i >= n) continue;
+    if (fast) {
+      for (int jj = l; jj < cnt; jj += L) {
+        if (j0 + jj == i) continue;
+        const double dx = sh_pos[3 * jj] - xi;
+        const double dy = sh_pos[3 * jj + 1] - yi;
+        const double dz = sh_pos[3 * jj + 2] - zi;
+        double r3 = rinv3_f64(fma(dz, dz, fma(dy, dy, fma(dx, dx, eps2))));
+        if (masses) r3 *= sh_m[jj];
+        sx = fma(dx, r3, sx);
+        sy = fma(dy, r3, sy);
+        sz = fma(dz, r3, sz);
+      }
+    } else {
       for (int jj = l; jj < cnt; jj += L) {
         const long long j = j0 + jj;
         if (j == i) continue;
@@ -420,15 +438,45 @@ constexpr int jp_smem_bytes() {
   return 2 * (int)sizeof(PartnerPair) * T + 2 * T * (int)sizeof(PackedBody);
 }
 
+// Bounding box of a tile of packed positions (FP32 hi parts relative to the
+// reference point): centre (x, y, z) and a radius (w) that bounds every hi
+// point's distance from the rounded centre.
+struct TileBox {
+  float4 c;
+};
+
+// True when no pair of the i-tile (box I, every body within |h_i| / 8 <=
+// ti of the reference point's near-pair threshold) and the j-tile (box J)
+// can be a close pair of the packed loop (r^2 < (|h_i| / 8)^2): the boxes'
+// gap exceeds ti.  The margins (1e-5 relative) cover the FP32 rounding of
+// this test and of the loop's r^2 and thresholds, so a far tile gives
+// exactly the terms the close-pair test would (none revisited).
+__device__ __forceinline__ bool tiles_far(float4 I, float ti, float4 J) {
+  const float dx = I.x - J.x, dy = I.y - J.y, dz = I.z - J.z;
+  const float d = __fsqrt_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))));
+  return __fmul_rn(d, 1.0f - 1e-5f) - I.w - J.w > __fmul_rn(ti, 1.0f + 1e-5f);
+}
+
 // PAIRS (one lane per body): part is read as float2[BI][3] and receives each
 // sum as its FP32 Kahan pair (s, -c), value s - c, with no FP64 arithmetic.
-template <int T, int L, int NB = 1, bool PAIRS = false>
+// CULL (one lane and one body per thread, 128 threads, partner ranges that
+// start at multiples of 128): boxes[t] bounds the packed positions of bodies
+// [128 t, 128 t + 128) and ibox the CTA's own; every 128-partner half of a
+// tile that tiles_far separates from the i-tile runs the pair loop without
+// the close-pair test.  Its terms are the ones the test would have kept, so
+// the sums are bit for bit those of the loop with the test.
+template <int T, int L, int NB = 1, bool PAIRS = false, bool CULL = false>
 __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict__ packed,
                                                    long long n, long long i0, long long jb,
                                                    long long je, float eps2, unsigned char* smem,
-                                                   double (*part)[3]) {
+                                                   double (*part)[3],
+                                                   const float4* __restrict__ boxes = nullptr,
+                                                   float4 ibox = float4{}) {
+  static_assert(!CULL || (L == 1 && NB == 1 && T == 128), "culling: 128 one-body threads");
   constexpr int BG = T / L;  // body groups per CTA (NB bodies each)
   constexpr int JT = 2 * T;  // partners per tile
+  __shared__ int sh_far[2][2];   // far flags of the two 128-partner halves, per buffer
+  __shared__ float4 sh_ibox[2];  // i-tile box, near-pair bound of its bodies
   PartnerPair* recs = reinterpret_cast<PartnerPair*>(smem);  // two buffers of T records
   PackedBody* raw = reinterpret_cast<PackedBody*>(smem + 2 * sizeof(PartnerPair) * T);
   const int g = threadIdx.x / L;
@@ -475,8 +523,26 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     }
     cp_async_commit();
   };
+  if constexpr (CULL) {
+    if (threadIdx.x == 0) {
+      sh_ibox[0] = ibox;
+      // |h_i| <= |c_I| + R_I for every body of the tile: the near-pair
+      // threshold |h_i| / 8 is at most that over 8
+      const float ci = __fsqrt_rn(__fmaf_rn(ibox.z, ibox.z,
+                                            __fmaf_rn(ibox.y, ibox.y, __fmul_rn(ibox.x, ibox.x))));
+      sh_ibox[1].x = __fmul_rn(ci + ibox.w, 0.125f);
+    }
+    __syncthreads();
+  }
   auto build = [&](long long j0, PartnerPair* out) {
     const int cnt = (int)min((long long)JT, je - j0);
+    if constexpr (CULL) {
+      if (threadIdx.x < 2) {
+        const long long h0 = j0 + 128 * (long long)threadIdx.x;
+        sh_far[out == recs ? 0 : 1][threadIdx.x] =
+            h0 < je ? (int)tiles_far(sh_ibox[0], sh_ibox[1].x, boxes[h0 / 128]) : 0;
+      }
+    }
     if ((int)threadIdx.x < (cnt + 1) / 2) {
       const PackedBody a = raw[2 * threadIdx.x];
       PackedBody b;
@@ -516,6 +582,29 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     const int kn = (npair - l + L - 1) / L;
     for (int k0 = 0; k0 < kn; k0 += 32) {
       const int kc = min(32, kn - k0);
+      if constexpr (CULL) {
+        // records [0, 64) hold partners of the first 128-body half
+        if (sh_far[buf][k0 >= 64 ? 1 : 0]) {
+#pragma unroll 4
+          for (int u = 0; u < kc; ++u) {
+            const int jj = k0 + u;
+            const ulonglong2 xy = rec[jj].xy;
+            const f2_t hz = rec[jj].zl.x;
+            const f2_t dx = f2_sub(xy.x, HX[0]);
+            const f2_t dy = f2_sub(xy.y, HY[0]);
+            const f2_t dz = f2_sub(hz, HZ[0]);
+            const f2_t r2 = f2_fma(dz, dz, f2_fma(dy, dy, f2_fma(dx, dx, E2)));
+            float ra, rb;
+            f2_unpack(r2, ra, rb);
+            const f2_t ri = f2_pack(rsqrt_sfu(ra), rsqrt_sfu(rb));
+            const f2_t sc = f2_mul(ri, f2_mul(ri, ri));
+            TX[0] = f2_fma(sc, dx, TX[0]);
+            TY[0] = f2_fma(sc, dy, TY[0]);
+            TZ[0] = f2_fma(sc, dz, TZ[0]);
+          }
+          continue;
+        }
+      }
       unsigned mask = 0;
 #pragma unroll(4 / NB)
       for (int u = 0; u < kc; ++u) {

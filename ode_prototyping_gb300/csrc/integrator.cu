@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 5 * 128 / T)
     if constexpr (PREC == GB_PREC_F64) {
       double* sh_pos = reinterpret_cast<double*>(sh_raw);
       double* sh_m = sh_pos + 3 * T;
-      force_f64_cta<T, L>(ysrc, n, i0, jb, je, P.eps2, P.masses, sh_pos, sh_m, part);
+      force_f64_cta<T, L>(ysrc, n, i0, jb, je, P.eps2, P.masses, sh_pos, sh_m, part,
+                          P.f64_fast != 0);
     } else {
       const PackedBody* src = (s == 0) ? P.PX + (long long)px * n : P.PY + (long long)(s & 1) * n;
       if constexpr (PACKED) {
@@ -135,22 +136,202 @@ __global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 5 * 128 / T)
   if (threadIdx.x == 0) P.partials[ci.itile * ci.size + ci.rank] = tile_sum;
 }
 
-// The packed mixed stage as independent (i-tile, partner chunk) CTAs, without
-// clusters.  Cluster-bound CTAs of one launch drain each SM from seven resident
-// CTAs to one, because the warp schedulers favour older CTAs (measured at
-// N = 16384: identical CTAs finished their pair loops between 45 and 128 us),
-// and an 8-CTA cluster waits for its slowest rank; independent CTAs let the
-// block scheduler refill every SM until the last chunks.  Each CTA stores its
-// chunk's sums as FP32 Kahan pairs; the CTA whose arrival completes the tile's
-// count (an atomic increment, nothing waits) adds the chunks in chunk order,
-// so the sums do not depend on which CTA arrives last, resets the count for
-// the next launch and finishes the tile.
+// Box of a sorted tile's new packed positions, by the CTA that finishes the
+// tile: min / max of the hi parts over its cnt bodies (warp shuffles, then
+// the four warps in shared memory), centre and a radius rounded outwards so
+// that it bounds every hi point's distance from the rounded centre.  The load
+// (box_load, one body per thread) is issued early; box_write reduces and
+// writes.  All 128 threads must call box_write.
+__device__ __forceinline__ float4 box_load(const PackedBody* __restrict__ p, int cnt) {
+  return (int)threadIdx.x < cnt ? __ldcg(&p[threadIdx.x].hw)
+                                : make_float4(nanf(""), 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ void box_write(float4 h, float4* out, float* red) {
+  const bool valid = !isnan(h.x);
+  float v[6];
+  if (valid) {
+    v[0] = h.x; v[1] = h.y; v[2] = h.z;
+    v[3] = -h.x; v[4] = -h.y; v[5] = -h.z;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) v[k] = 3.0e38f;
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) red[6 * w + k] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = fminf(fminf(red[k], red[6 + k]), fminf(red[12 + k], red[18 + k]));
+      hi[k] = -fminf(fminf(red[3 + k], red[9 + k]), fminf(red[15 + k], red[21 + k]));
+    }
+    float4 b;
+    b.x = 0.5f * (lo[0] + hi[0]);
+    b.y = 0.5f * (lo[1] + hi[1]);
+    b.z = 0.5f * (lo[2] + hi[2]);
+    const float ex = 0.5f * (hi[0] - lo[0]), ey = 0.5f * (hi[1] - lo[1]),
+                ez = 0.5f * (hi[2] - lo[2]);
+    const float r = __fsqrt_ru(__fmaf_ru(ez, ez, __fmaf_ru(ey, ey, __fmul_ru(ex, ex))));
+    b.w = r * 1.00001f + 3.0e-7f * (fabsf(b.x) + fabsf(b.y) + fabsf(b.z));
+    *out = b;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void write_tile_box(const PackedBody* __restrict__ p, int cnt,
+                                               float4* out, float* red) {
+  box_write(box_load(p, cnt), out, red);
+}
+
+// One CTA of 128 threads per tile: packs the positions of x0 (ring slot
+// *cur) in the order perm into out[*slot] and writes the tile boxes.
+__global__ void __launch_bounds__(128)
+    pack_boxes_kernel(const double* __restrict__ ring, const int* cur, long long n_var,
+                      long long n, const int* __restrict__ perm, const double* __restrict__ cref,
+                      PackedBody* out, const int* slot, float4* boxes, long long n_tiles) {
+  __shared__ float red[32];
+  const double* x = ring + (long long)*cur * n_var;
+  PackedBody* o = out + (long long)*slot * n;
+  const long long i0 = (long long)blockIdx.x * 128;
+  const int cnt = (int)min(128LL, n - i0);
+  if ((int)threadIdx.x < cnt) {
+    const long long id = perm[i0 + threadIdx.x];
+    o[i0 + threadIdx.x] =
+        pack_body(x[3 * id], x[3 * id + 1], x[3 * id + 2], cref[0], cref[1], cref[2], 1.0f);
+  }
+  __threadfence_block();
+  __syncthreads();
+  write_tile_box(o + i0, cnt, boxes + (long long)*slot * n_tiles + blockIdx.x, red);
+}
+
+__global__ void iota_kernel(int* p, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = (int)i;
+}
+
+// Rows [rb, rb + cnt) of a sorted i-tile (bodies perm[i0 + rb ..]) before the
+// stage's pair loop: everything of the stage combination that does not need
+// this stage's accelerations.  The position elements are finished here (their
+// stage derivative is the stage state's velocity): k_s, the next stage state
+// (or, at the last stage, the candidate state, its error, target and scaled
+// square) and the packed hi/lo positions of the next stage at their sorted
+// places.  The velocity elements get their sums over the earlier stages, in
+// the ascending order the whole sum uses, so the tile's last CTA adds only
+// the last term.  Every thread of the CTA must call it.
+template <int T>
+__device__ __forceinline__ void split_pre_rows(const DevTableau& tab, const FusedParams& P,
+                                               const Ctrl* C, int s, long long i0, int rb,
+                                               int cnt, double* sh_pos, double& sq_acc) {
+  const int S = tab.n_stages;
+  const bool last = (s == S - 1);
+  const long long n = P.n, n_var = P.n_var;
+  const int k0slot = C->k0slot;
+  const double dt = C->dt;
+  const int cur = C->cur;
+  const double* x0 = P.ring + (long long)cur * n_var;
+  const double* ysrc = (s == 0) ? x0 : P.Y + (long long)(s & 1) * n_var;
+  const int h3 = 3 * cnt;
+  double* ks_s = P.ks + (long long)kslot(s, S, k0slot) * n_var;
+  for (int v = threadIdx.x; v < 2 * h3; v += T) {
+    const bool pos = v < h3;
+    const int w = pos ? v : v - h3;
+    const long long body = P.perm[i0 + rb + w / 3];
+    const long long e3 = 3 * body + w % 3;  // element of the 3N half
+    const long long idx = (pos ? 0 : 3 * n) + e3;
+    double ks_now = 0.0;
+    if (pos) {
+      ks_now = ysrc[3 * n + idx];  // dx/dt = v of the stage state
+      ks_s[idx] = ks_now;
+    }
+    // every term's load in flight at once (this runs before the pair loop,
+    // whose registers are not live yet), then the sum in stage order
+    double kl[GB_MAX_STAGES];
+    if (!last) {
+      const unsigned m = tab.anz[s];
+#pragma unroll
+      for (int l = 0; l < GB_MAX_STAGES; ++l)
+        if (l < s && ((m >> l) & 1u)) kl[l] = P.ks[(long long)kslot(l, S, k0slot) * n_var + idx];
+      double acc = 0.0;
+#pragma unroll
+      for (int l = 0; l < GB_MAX_STAGES; ++l)
+        if (l < s && ((m >> l) & 1u)) acc = dadd(acc, dmul(tab.a[s][l], kl[l]));
+      if (pos) {
+        if ((m >> s) & 1u) acc = dadd(acc, dmul(tab.a[s][s], ks_now));
+        const double y = dadd(x0[idx], dmul(acc, dt));
+        P.Y[(long long)((s + 1) & 1) * n_var + idx] = y;
+        sh_pos[w] = y;
+      } else {
+        P.pre[e3] = acc;
+      }
+    } else {
+      const unsigned mb = tab.bnz, md = tab.dbnz, m = mb | md;
+      const int lend = pos ? S : S - 1;  // velocity elements: all but the last stage
+#pragma unroll
+      for (int l = 0; l < GB_MAX_STAGES; ++l)
+        if (l < lend && ((m >> l) & 1u))
+          kl[l] = (l == s) ? ks_now : P.ks[(long long)kslot(l, S, k0slot) * n_var + idx];
+      double xv = 0.0, ev = 0.0;
+#pragma unroll
+      for (int l = 0; l < GB_MAX_STAGES; ++l) {
+        if (l >= lend) break;
+        if ((mb >> l) & 1u) xv = dadd(xv, dmul(tab.b[l], kl[l]));
+        if ((md >> l) & 1u) ev = dadd(ev, dmul(tab.db[l], kl[l]));
+      }
+      if (pos) {
+        const double x0e = x0[idx];
+        const double xn = dadd(x0e, dmul(xv, dt));
+        const double er = dmul(ev, dt);
+        P.ring[(long long)((cur + 1) % P.R) * n_var + idx] = xn;
+        const double at = P.atol ? P.atol[idx] : P.atol_s;
+        const double rt = P.rtol ? P.rtol[idx] : P.rtol_s;
+        const double ax = fabs(xn), ax0 = fabs(x0e);
+        const double tg = dadd(at, dmul(rt, ax < ax0 ? ax0 : ax));
+        const double q = __ddiv_rn(er, tg);
+        sq_acc = dadd(sq_acc, dmul(q, q));
+        sh_pos[w] = xn;
+      } else {
+        P.pre[e3] = xv;
+        P.pre[3 * n + e3] = ev;
+      }
+    }
+  }
+  __syncthreads();
+  PackedBody* dst = last ? P.PX + (long long)(C->px ^ 1) * n : P.PY + (long long)((s + 1) & 1) * n;
+  for (int r = threadIdx.x; r < cnt; r += T) {
+    const double* p = sh_pos + 3 * r;
+    dst[i0 + rb + r] = pack_body(p[0], p[1], p[2], P.cref[0], P.cref[1], P.cref[2], 1.0f);
+  }
+}
+
+// The packed mixed stage (uniform masses, from N = 8192) as independent
+// (i-tile, partner chunk) CTAs on Morton-sorted bodies.  Clusters are not
+// used: cluster-bound CTAs of one launch drained each SM from seven resident
+// CTAs to one (the warp schedulers favour older CTAs: identical CTAs finished
+// their pair loops between 45 and 128 us at N = 16384) while an 8-CTA cluster
+// waited for its slowest rank; independent CTAs let the block scheduler
+// refill every SM until the last chunks.  Each CTA first finishes its slice
+// of the tile's rows as far as this stage's accelerations allow
+// (split_pre_rows), then runs the pair loop, in which every 128-partner half
+// tile whose box is far from the i-tile's skips the close-pair test (sorted
+// tiles are compact, so most are), and stores its chunk's sums as FP32 Kahan
+// pairs.  The CTA whose arrival completes the tile's count (an atomic
+// increment; nothing waits) adds the chunks in chunk order, so the sums do
+// not depend on which CTA arrives last, resets the count for the next launch,
+// adds the last term of every velocity element and writes the box of the
+// tile's new positions for the next stage.
 template <int T, int L, int BPT>
 __global__ void __launch_bounds__(T, 7 * 128 / T)
     fused_split_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ FusedParams P, int s) {
-  static_assert(L == 1, "partner chunks: one lane per body");
-  constexpr int BI = (T / L) * BPT;
+  static_assert(L == 1 && BPT == 1 && T == 128, "partner chunks: 128 one-body threads");
+  constexpr int BI = T;
   constexpr int BW = BI * 3;  // sums of one chunk (8 bytes each)
   __shared__ __align__(16) unsigned char sh_raw[jp_smem_bytes<T>()];
   __shared__ double part[BI][3];
@@ -165,83 +346,182 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
   const int chunk = (int)(blockIdx.x / P.n_itiles);
   const long long n = P.n, n_var = P.n_var;
   const long long i0 = itile * BI;
-  const bool skip_force = (s == 0 && C->k0_valid);
-  if (skip_force) {
-    if (chunk != 0) return;  // the stage derivative is reused: one CTA per tile
-  } else {
-    const long long jb = P.chunk_start[chunk], je = P.chunk_start[chunk + 1];
-    const PackedBody* src =
-        (s == 0) ? P.PX + (long long)C->px * n : P.PY + (long long)(s & 1) * n;
-    force_mixed_cta_jp<T, L, BPT, true>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
-    __syncthreads();
-    // the chunk's sums leave as FP32 Kahan pairs (s, -c)
-    const float2* pf = reinterpret_cast<const float2*>(&part[0][0]);
-    float2* mine = reinterpret_cast<float2*>(P.chunk_sums) + (itile * nc + chunk) * BW;
-    for (int e = threadIdx.x; e < BW; e += T) mine[e] = pf[e];
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) sh_last = atomicAdd(P.tile_count + itile, 1u) == (unsigned)(nc - 1);
-    __syncthreads();
-    if (!sh_last) return;
-    __threadfence();
-    // chunks added in chunk order in double-single FP32 arithmetic (the FP64
-    // pipe runs at 1/64 of the FP32 rate), one conversion per component
-    const float2* g0 = reinterpret_cast<const float2*>(P.chunk_sums) + itile * nc * BW;
-    double* pw = &part[0][0];
-    for (int e = threadIdx.x; e < BW; e += T) {
-      float S = 0.f, E = 0.f;
-      for (int c = 0; c < nc; ++c) {
-        const float2 v = __ldcg(g0 + (long long)c * BW + e);
-        ds_add(S, E, v.x, v.y);
-      }
-      pw[e] = dadd((double)S, (double)E);
-    }
-    if (threadIdx.x == 0) P.tile_count[itile] = 0u;
-    __syncthreads();
-  }
-  const int cur = C->cur;
-  const int px = C->px;
   const int S = tab.n_stages;
   const bool last = (s == S - 1);
-  const double* x0 = P.ring + (long long)cur * n_var;
-  EpiCtx E;
-  E.tab = &tab;
-  E.s = s;
-  E.S = S;
-  E.k0slot = C->k0slot;
-  E.skip_force = skip_force;
-  E.last = last;
-  E.exact = P.exact != 0;
-  E.dt = C->dt;
-  E.n = n;
-  E.x0 = x0;
-  E.ysrc = (s == 0) ? x0 : P.Y + (long long)(s & 1) * n_var;
-  E.ks = P.ks;
-  E.kstride = n_var;
-  E.ynext = P.Y + (long long)((s + 1) & 1) * n_var;
-  E.xnew = P.ring + (long long)((cur + 1) % P.R) * n_var;
-  E.pnext = last ? P.PX + (long long)(px ^ 1) * n : P.PY + (long long)((s + 1) & 1) * n;
-  E.atol = P.atol;
-  E.rtol = P.rtol;
-  E.atol_s = P.atol_s;
-  E.rtol_s = P.rtol_s;
-  E.masses = P.masses;
-  E.mass = P.mass;
-  E.cref = P.cref;
-  E.sq = P.sq;
+  const bool skip_force = (s == 0 && C->k0_valid);
   const int b_hi = (int)min((long long)BI, n - i0);
-  double sq_acc = 0.0;
-  double amax = 0.0;
-#pragma unroll 1
-  for (int b = threadIdx.x; b < b_hi; b += T)
-    body_epilogue<GB_PREC_MIXED>(E, i0 + b, part[b], sq_acc, amax);
-  if (last) {
-    const double m = block_max(amax, red);
-    if (threadIdx.x == 0) P.aux[itile] = m;
+  PackedBody* pnext = last ? P.PX + (long long)(C->px ^ 1) * n : P.PY + (long long)((s + 1) & 1) * n;
+  float4* box_next = last ? P.BX + (long long)(C->px ^ 1) * P.n_itiles
+                          : P.BY + (long long)((s + 1) & 1) * P.n_itiles;
+  if (skip_force) {
+    // the stage derivative is reused: one CTA per tile runs the whole epilogue
+    if (chunk != 0) return;
+    const int cur = C->cur;
+    const double* x0 = P.ring + (long long)cur * n_var;
+    EpiCtx E;
+    E.tab = &tab;
+    E.s = s;
+    E.S = S;
+    E.k0slot = C->k0slot;
+    E.skip_force = true;
+    E.last = last;
+    E.exact = false;
+    E.dt = C->dt;
+    E.n = n;
+    E.x0 = x0;
+    E.ysrc = x0;
+    E.ks = P.ks;
+    E.kstride = n_var;
+    E.ynext = P.Y + (long long)((s + 1) & 1) * n_var;
+    E.xnew = P.ring + (long long)((cur + 1) % P.R) * n_var;
+    E.pnext = nullptr;
+    E.atol = P.atol;
+    E.rtol = P.rtol;
+    E.atol_s = P.atol_s;
+    E.rtol_s = P.rtol_s;
+    E.masses = nullptr;
+    E.mass = P.mass;
+    E.cref = P.cref;
+    E.sq = nullptr;
+    double sq_acc = 0.0, amax = 0.0;
+    if ((int)threadIdx.x < b_hi) {
+      double np[3];
+      body_epilogue<GB_PREC_MIXED>(E, P.perm[i0 + threadIdx.x], part[threadIdx.x], sq_acc, amax,
+                                   np);
+      pnext[i0 + threadIdx.x] = pack_body(np[0], np[1], np[2], P.cref[0], P.cref[1], P.cref[2],
+                                          1.0f);
+    }
+    __threadfence_block();
+    __syncthreads();
+    write_tile_box(pnext + i0, b_hi, box_next + itile, reinterpret_cast<float*>(red));
+    return;
   }
+  {
+    // this chunk's slice of the tile's rows, before the pair loop
+    const int rpc = (BI + nc - 1) / nc;
+    const int rb = chunk * rpc;
+    const int cnt = max(0, min(b_hi, rb + rpc) - rb);
+    double sq_pos = 0.0;
+    split_pre_rows<T>(tab, P, C, s, i0, rb, cnt, &part[0][0], sq_pos);
+    if (last) {
+      const double v = block_sum(sq_pos, red);
+      if (threadIdx.x == 0) P.partials[itile * (nc + 1) + chunk] = v;
+    }
+    __syncthreads();  // part (the slice's positions) is free for the pair sums
+  }
+  const long long jb = P.chunk_start[chunk], je = P.chunk_start[chunk + 1];
+  const PackedBody* src = (s == 0) ? P.PX + (long long)C->px * n : P.PY + (long long)(s & 1) * n;
+  const float4* boxes = (s == 0) ? P.BX + (long long)C->px * P.n_itiles
+                                 : P.BY + (long long)(s & 1) * P.n_itiles;
+  if (P.cull) {
+    force_mixed_cta_jp<T, L, BPT, true, true>(src, n, i0, jb, je, P.eps2f, sh_raw, part, boxes,
+                                              boxes[itile]);
+  } else {
+    force_mixed_cta_jp<T, L, BPT, true>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
+  }
+  __syncthreads();
+  // the chunk's sums leave as FP32 Kahan pairs (s, -c)
+  const float2* pf = reinterpret_cast<const float2*>(&part[0][0]);
+  float2* mine = reinterpret_cast<float2*>(P.chunk_sums) + (itile * nc + chunk) * BW;
+  for (int e = threadIdx.x; e < BW; e += T) mine[e] = pf[e];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) sh_last = atomicAdd(P.tile_count + itile, 1u) == (unsigned)(nc - 1);
+  __syncthreads();
+  if (!sh_last) return;
+  __threadfence();
+  // What the tile's velocity elements need is loaded first, so its latency
+  // overlaps the chunk sums: element e = threadIdx.x + 128 r of the tile's 3 x
+  // 128 acceleration components, its state index, x0, the earlier stages'
+  // sums, and the box input (the tile's new packed positions).
+  const int k0slot = C->k0slot;
+  const double dt = C->dt;
+  const int cur = C->cur;
+  const double* x0 = P.ring + (long long)cur * n_var;
+  double* ks_s = P.ks + (long long)kslot(s, S, k0slot) * n_var;
+  const int ne = 3 * b_hi;
+  long long wv[3];
+  double x0v[3], p1[3], p2[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int e = (int)threadIdx.x + r * T;
+    wv[r] = e < ne ? 3 * (long long)P.perm[i0 + e / 3] + e % 3 : 0;
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int e = (int)threadIdx.x + r * T;
+    if (e < ne) {
+      x0v[r] = x0[3 * n + wv[r]];
+      p1[r] = P.pre[wv[r]];
+      p2[r] = last ? P.pre[3 * n + wv[r]] : 0.0;
+    }
+  }
+  const float4 bx = box_load(pnext + i0, b_hi);
+  // chunks added in chunk order in double-single FP32 arithmetic (the FP64
+  // pipe runs at 1/64 of the FP32 rate), eight loads in flight at a time,
+  // one conversion per component
+  const float2* g0 = reinterpret_cast<const float2*>(P.chunk_sums) + itile * nc * BW;
+  double* pw = &part[0][0];
+  double acc[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int e = (int)threadIdx.x + r * T;
+    float hs = 0.f, ls = 0.f;
+    for (int c0 = 0; c0 < nc; c0 += 8) {
+      float2 vv[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c0 + c < nc) vv[c] = __ldcg(g0 + (long long)(c0 + c) * BW + e);
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c0 + c < nc) ds_add(hs, ls, vv[c].x, vv[c].y);
+    }
+    acc[r] = dadd((double)hs, (double)ls);
+    pw[e] = acc[r];
+  }
+  if (threadIdx.x == 0) P.tile_count[itile] = 0u;
+  // the velocity elements: k_s = m a, plus the last term of each sum
+  double sq_acc = 0.0;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int e = (int)threadIdx.x + r * T;
+    if (e >= ne) continue;
+    const long long idx = 3 * n + wv[r];
+    const double k = dmul(acc[r], P.mass);
+    ks_s[idx] = k;
+    if (!last) {
+      double v = p1[r];
+      if ((tab.anz[s] >> s) & 1u) v = dadd(v, dmul(tab.a[s][s], k));
+      P.Y[(long long)((s + 1) & 1) * n_var + idx] = dadd(x0v[r], dmul(v, dt));
+    } else {
+      double xv = p1[r], ev = p2[r];
+      if ((tab.bnz >> s) & 1u) xv = dadd(xv, dmul(tab.b[s], k));
+      if ((tab.dbnz >> s) & 1u) ev = dadd(ev, dmul(tab.db[s], k));
+      const double xn = dadd(x0v[r], dmul(xv, dt));
+      const double er = dmul(ev, dt);
+      P.ring[(long long)((cur + 1) % P.R) * n_var + idx] = xn;
+      const double at = P.atol ? P.atol[idx] : P.atol_s;
+      const double rt = P.rtol ? P.rtol[idx] : P.rtol_s;
+      const double ax = fabs(xn), ax0 = fabs(x0v[r]);
+      const double tg = dadd(at, dmul(rt, ax < ax0 ? ax0 : ax));
+      const double q = __ddiv_rn(er, tg);
+      sq_acc = dadd(sq_acc, dmul(q, q));
+    }
+  }
+  box_write(bx, box_next + itile, reinterpret_cast<float*>(red));
   if (!last) return;
+  double amax = 0.0;
+  for (int b = threadIdx.x; b < b_hi; b += T) {
+    const double k0 = dmul(pw[3 * b], P.mass), k1 = dmul(pw[3 * b + 1], P.mass),
+                 k2 = dmul(pw[3 * b + 2], P.mass);
+    amax = fmax(amax, sqrt(k0 * k0 + k1 * k1 + k2 * k2));
+  }
+  const double m = block_max(amax, red);
   const double tile_sum = block_sum(sq_acc, red);
-  if (threadIdx.x == 0) P.partials[itile] = tile_sum;
+  if (threadIdx.x == 0) {
+    P.aux[itile] = m;
+    P.partials[itile * (nc + 1) + nc] = tile_sum;
+  }
 }
 
 // The mixed-precision stage on Morton-sorted tiles: i-tile = 128 consecutive
@@ -721,6 +1001,10 @@ struct gb_integrator_s {
   void* mlp_dev = nullptr;
   double* chunk_sums = nullptr;
   unsigned* tile_count = nullptr;
+  double* pre = nullptr;
+  float4* BX = nullptr;
+  float4* BY = nullptr;
+  bool split_sort = false;          // split stage on Morton-sorted bodies
   // host
   gb::Ctrl* hctrl = nullptr;  // pinned
   double* hstage = nullptr;   // pinned R * n_var (recording)
@@ -759,7 +1043,7 @@ void free_all(gb_integrator_s* it) {
                   it->sq,    it->dscal, it->norm_work, it->masses, it->log,      it->mlp_dev,
                   it->perm,  it->vals, it->keys,     it->keys_alt, it->cub_temp, it->bbox,
                   it->PXF,   it->PYF,  it->MX,       it->MY,       it->dense_t, it->dense_out,
-                  it->chunk_sums, it->tile_count};
+                  it->chunk_sums, it->tile_count, it->pre, it->BX, it->BY};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (it->hctrl) cudaFreeHost(it->hctrl);
@@ -769,12 +1053,28 @@ void free_all(gb_integrator_s* it) {
   if (it->stream && it->own_stream) cudaStreamDestroy(it->stream);
 }
 
-// Partner chunk boundaries of the split stage kernel: nc chunks of equal
-// length in partner pairs (the packed loop takes any run of pairs).
+// Partner chunk boundaries of the split stage kernel, each a multiple of 128
+// partners (a tile of the box test; the packed loop takes any run of pairs).
+// CTAs are dispatched chunk-major, so the last chunks are the last work of
+// the launch: their lengths fall off, in the weights 6 (first half of the
+// chunks), 4, 2 (an eighth each) and 1 (the rest), so that the SMs drain on
+// short CTAs (measured at N = 16384, 16 chunks: 0.1350 ms per RKF78 stage
+// against 0.1384 ms for equal chunks; 8 or 32 chunks, equal or falling, were
+// no faster).
 std::vector<long long> split_schedule(long long n, int nc) {
-  const long long pairs = (n + 1) / 2, per = (pairs + nc - 1) / nc;
-  std::vector<long long> b;
-  for (int c = 0; c < nc; ++c) b.push_back(std::min(n, 2 * per * c));
+  const long long tiles = (n + 127) / 128;
+  std::vector<long long> w((size_t)nc), b;
+  const int h = nc / 2, e = nc / 8;
+  long long total = 0;
+  for (int c = 0; c < nc; ++c) {
+    w[c] = c < h ? 6 : (c < h + e ? 4 : (c < h + 2 * e ? 2 : 1));
+    total += w[c];
+  }
+  long long acc = 0;
+  for (int c = 0; c < nc; ++c) {
+    b.push_back(std::min(n, 128 * (tiles * acc / total)));
+    acc += w[c];
+  }
   b.push_back(n);
   return b;
 }
@@ -801,8 +1101,26 @@ int launch_fused(gb_integrator_s* it, int s) {
   return GB_OK;
 }
 
-// Re-sorts the bodies of x0 along a Morton curve and repacks x0's tiles.
+// Re-sorts the bodies of x0 along a Morton curve and repacks x0's tiles (and
+// their boxes, split stage).
 int launch_resort(gb_integrator_s* it) {
+  if (it->split) {
+    cudaStream_t s = it->stream;
+    const int* cur = reinterpret_cast<const int*>(reinterpret_cast<const char*>(it->ctrl) +
+                                                  offsetof(Ctrl, cur));
+    const int* px = reinterpret_cast<const int*>(reinterpret_cast<const char*>(it->ctrl) +
+                                                 offsetof(Ctrl, px));
+    if (it->split_sort) {
+      SortBuffers sb{it->perm, it->vals, it->keys, it->keys_alt, it->cub_temp, it->cub_bytes,
+                     it->bbox};
+      GB_TRY(sort_bodies(it->ring, cur, it->n_var, it->n, sb, s));
+    }
+    pack_boxes_kernel<<<(unsigned)it->geom.n_itiles, 128, 0, s>>>(
+        it->ring, cur, it->n_var, it->n, it->perm, it->cref, it->PX, px, it->BX,
+        it->geom.n_itiles);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  }
   if (!it->sorted) return GB_OK;
   cudaStream_t s = it->stream;
   const long long n = it->n;
@@ -913,7 +1231,7 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   if (opts.precision == GB_PREC_F64) it->geom.BPT = 1;
   if (opts.precision == GB_PREC_MIXED && it->geom.T < 128) it->geom.T = 128;
   // spatially sorted tiles (mixed precision): on unless switched off
-  it->sorted = opts.precision == GB_PREC_MIXED && opts.spatial_sort > 0;
+  it->sorted = opts.precision == GB_PREC_MIXED && opts.spatial_sort == 1;
   if (it->sorted) {
     if (it->geom.L > 2) it->geom.L = 2;
     it->geom.BPT = it->geom.L;  // i-tile = j-tile = T bodies
@@ -923,7 +1241,7 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   // 1024 partners, at most 32 per tile (measured per RKF78 stage: N = 8192
   // 0.0563 ms against 0.0594 ms for clusters of 8 x 2 lanes; 16384 0.142
   // against 0.155; 32768 0.470 against 0.513; 131072 6.88 against 7.37).
-  if (!it->sorted && opts.precision == GB_PREC_MIXED && it->geom.variant != 1 && !opts.exact) {
+  if (!it->sorted && opts.precision == GB_PREC_MIXED && it->geom.variant == 3 && !opts.exact) {
     if (it->n >= 8192) {
       if (opts.tiling.lanes <= 0) it->geom.L = 1;
       if (it->geom.L == 1 && opts.tiling.j_split <= 0) {
@@ -932,18 +1250,19 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
         it->geom.P = P;
       }
     }
-    it->split = it->geom.L == 1 && it->geom.P > 1;
+    it->split = it->geom.L == 1 && it->geom.P > 1 && it->geom.T == 128 && it->geom.BPT == 1;
     if (it->split) {
       it->chunks = split_schedule(it->n, std::min(it->geom.P, kMaxChunks));
       it->geom.P = (int)it->chunks.size() - 1;
+      // spatial_sort 3: bodies in their own order (no Morton sort)
+      it->split_sort = opts.spatial_sort != 3;
     }
   }
   it->geom.n_itiles = (it->n + it->geom.bodies_per_cta() - 1) / it->geom.bodies_per_cta();
   it->kernel = it->sorted ? pick_sorted(it->geom.T, it->geom.L, sys->masses_dev == nullptr)
                           : pick_fused(opts.precision, it->geom.T, it->geom.L, it->geom.BPT,
                                        it->geom.variant != 1);
-  if (it->split)
-    it->kernel = it->geom.BPT == 1 ? pick_split<1>(it->geom.L) : pick_split<2>(it->geom.L);
+  if (it->split) it->kernel = pick_split<1>(it->geom.L);
   it->start_tiling = opts.tiling;
   if (it->start_tiling.j_split > 8) it->start_tiling.j_split = 8;
   int rc = GB_OK;
@@ -973,8 +1292,9 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   GB_ALLOC(it->ks, (size_t)it->S * nv * sizeof(double));
   GB_ALLOC(it->Y, (size_t)2 * nv * sizeof(double));
   GB_ALLOC(it->cref, 4 * sizeof(double));
-  // one partial per (i-tile, cluster rank); entries a kernel does not write stay 0
-  const size_t n_parts = (size_t)it->geom.n_itiles * it->geom.P;
+  // one partial per (i-tile, cluster rank), or per (i-tile, chunk) plus one
+  // per i-tile in the split stage; entries a kernel does not write stay 0
+  const size_t n_parts = (size_t)it->geom.n_itiles * (it->geom.P + (it->split ? 1 : 0));
   GB_ALLOC(it->partials, n_parts * sizeof(double));
   GB_ALLOC(it->aux, n_parts * sizeof(double));
   e = cudaMemset(it->partials, 0, n_parts * sizeof(double));
@@ -983,6 +1303,22 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
     GB_ALLOC(it->chunk_sums, n_parts * 3 * (size_t)it->geom.bodies_per_cta() * sizeof(double));
     GB_ALLOC(it->tile_count, (size_t)it->geom.n_itiles * sizeof(unsigned));
     e = cudaMemset(it->tile_count, 0, (size_t)it->geom.n_itiles * sizeof(unsigned));
+    GB_ALLOC(it->pre, (size_t)nv * sizeof(double));
+    GB_ALLOC(it->BX, (size_t)2 * it->geom.n_itiles * sizeof(float4));
+    GB_ALLOC(it->BY, (size_t)2 * it->geom.n_itiles * sizeof(float4));
+    GB_ALLOC(it->perm, (size_t)n * sizeof(int));
+    if (e == cudaSuccess) {
+      iota_kernel<<<(unsigned)((n + 255) / 256), 256>>>(it->perm, n);
+      e = cudaGetLastError();
+    }
+    if (it->split_sort) {
+      GB_ALLOC(it->vals, (size_t)n * sizeof(int));
+      GB_ALLOC(it->keys, (size_t)n * sizeof(unsigned long long));
+      GB_ALLOC(it->keys_alt, (size_t)n * sizeof(unsigned long long));
+      GB_ALLOC(it->bbox, 8 * sizeof(double));
+      it->cub_bytes = sort_temp_bytes(n);
+      GB_ALLOC(it->cub_temp, it->cub_bytes);
+    }
   }
   if (e != cudaSuccess) {
     note_cuda_error(e);
@@ -1073,13 +1409,18 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
   P.n = n;
   P.n_var = nv;
   P.n_itiles = it->geom.n_itiles;
-  P.n_parts = it->split ? it->geom.n_itiles : it->geom.n_itiles * it->geom.P;
+  P.n_parts = (long long)n_parts;
+  P.pre = it->pre;
+  P.BX = it->BX;
+  P.BY = it->BY;
+  P.cull = opts.spatial_sort == 2 ? 0 : 1;
   P.n_chunks = it->split ? it->geom.P : 1;
   for (int c = 0; c <= kMaxChunks; ++c)
     P.chunk_start[c] = c < (int)it->chunks.size() ? it->chunks[c] : n;
   P.chunk_sums = it->chunk_sums;
   P.tile_count = it->tile_count;
   P.exact = opts.exact;
+  P.f64_fast = (opts.precision == GB_PREC_F64 && !opts.exact && opts.tiling.f64_pair != 2) ? 1 : 0;
   P.S = it->S;
   P.perm = it->perm;
   P.PXF = it->PXF;

@@ -82,14 +82,19 @@ struct FusedParams {
   const void* mlp;     // device MLP weights (learned controller) or null
   long long n, n_var, n_itiles, n_parts;
   int exact;
+  int f64_fast;        // FP64 stages: refined-rsqrt pair term (not exact mode)
   int S;
   // partner-chunk split without clusters (packed mixed path)
   int n_chunks;          // partner chunks per i-tile
   double* chunk_sums;    // n_itiles * n_chunks * 3 * bodies per tile, 8 bytes each
   unsigned* tile_count;  // n_itiles arrival counts, zero between launches
+  double* pre;           // n_var: velocity elements' sums over the earlier stages
+  float4* BX;            // 2 * n_itiles boxes of the packed x0 / x_new tiles (split stage)
+  float4* BY;            // 2 * n_itiles boxes of the packed stage-state tiles
+  int cull;              // split stage: far half tiles skip the close-pair test
   long long chunk_start[kMaxChunks + 1];  // partner range of chunk c: [start[c], start[c+1])
   // spatially sorted mixed path
-  const int* perm;       // sorted position -> body
+  const int* perm;       // sorted position -> body (spatially sorted and split paths)
   float4* PXF;           // 2 * n far records (x0 / x_new)
   float4* PYF;           // 2 * n far records (stage states)
   TileMeta* MX;          // 2 * n_itiles tile metadata (x0 / x_new)

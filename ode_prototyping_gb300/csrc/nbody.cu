@@ -28,7 +28,8 @@ __global__ void __launch_bounds__(T) rhs_f64_kernel(const double* __restrict__ p
                                                     double* __restrict__ out_vel,
                                                     double* __restrict__ out_acc, long long n,
                                                     double eps2, double mass,
-                                                    const double* __restrict__ masses, int mode) {
+                                                    const double* __restrict__ masses, int mode,
+                                                    int fast) {
   constexpr int BI = T / L;
   __shared__ double sh_pos[3 * T];
   __shared__ double sh_m[T];
@@ -37,7 +38,7 @@ __global__ void __launch_bounds__(T) rhs_f64_kernel(const double* __restrict__ p
   const long long i0 = ci.itile * BI;
   long long jb, je;
   j_chunk(n, ci.rank, ci.size, T, jb, je);
-  force_f64_cta<T, L>(pos, n, i0, jb, je, eps2, masses, sh_pos, sh_m, part);
+  force_f64_cta<T, L>(pos, n, i0, jb, je, eps2, masses, sh_pos, sh_m, part, fast != 0);
   cluster_combine<BI>(part, ci.rank, ci.size);
   if (ci.rank != 0) return;
   const long long nb = min((long long)BI, n - i0);
@@ -180,8 +181,11 @@ int run_f64(const double* pos, const double* vel, double* out_vel, double* out_a
   }
   if (!k) return GB_ERR_UNSUPPORTED;
   double eps2 = softening * softening;
+  // the standalone right-hand sides keep the reference's operation order
+  // unless the tiling asks for the refined-rsqrt pair term
+  int fast = (tiling && tiling->f64_pair == 1) ? 1 : 0;
   void* args[] = {(void*)&pos, (void*)&vel, (void*)&out_vel, (void*)&out_acc, (void*)&n,
-                  (void*)&eps2, (void*)&mass, (void*)&masses, (void*)&mode};
+                  (void*)&eps2, (void*)&mass, (void*)&masses, (void*)&mode, (void*)&fast};
   return launch_cluster(k, g, 0, s, args);
 }
 

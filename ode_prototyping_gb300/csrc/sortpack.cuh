@@ -118,6 +118,19 @@ inline size_t sort_temp_bytes(long long n) {
   return bytes;
 }
 
+// Bounding box, Morton keys and the radix sort: perm = bodies in Morton order.
+inline int sort_bodies(const double* base, const int* slot, long long stride, long long n,
+                       const SortBuffers& sb, cudaStream_t s) {
+  sort_bbox_kernel<<<1, 256, 0, s>>>(base, slot, stride, n, sb.bbox);
+  morton_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(base, slot, stride, n, sb.bbox,
+                                                             sb.keys, sb.vals);
+  GB_CUDA_TRY(cudaGetLastError());
+  size_t bytes = sb.cub_bytes;
+  GB_CUDA_TRY(cub::DeviceRadixSort::SortPairs(sb.cub_temp, bytes, sb.keys, sb.keys_alt, sb.vals,
+                                              sb.perm, (int)n, 0, 63, s));
+  return GB_OK;
+}
+
 // Bounding box, Morton keys, radix sort (perm), then the tile packing.
 inline int sort_and_pack(const double* base, const int* slot, long long stride, long long n,
                          const SortBuffers& sb, const double* masses, const double* cref,

@@ -110,6 +110,7 @@ def lib() -> C.CDLL:
         _lib.orc_tableau_builtin.argtypes = [C.c_int, C.POINTER(Tableau)]
         _lib.orc_dopri5_dense_eval.argtypes = [_DP, _DP, _DP, C.c_int64, C.c_double,
                                                C.c_double, _DP, C.c_int64, _DP]
+        _lib.orc_ic_plummer.argtypes = [C.c_int64, C.c_uint64, C.c_double, _DP]
         _lib.orc_pi_sequence.argtypes = [C.c_double] * 5 + [_DP, C.c_int64, C.c_double, _DP]
         _lib.orc_session_set_controller.argtypes = [C.c_void_p, C.c_int, C.c_double]
         _lib.orc_session_set_dense.argtypes = [C.c_void_p, _DP, C.c_int64, _DP]
@@ -174,6 +175,14 @@ def dopri5_dense(y0, y1, ks, h: float, t_new: float, ts) -> np.ndarray:
     assert lib().orc_dopri5_dense_eval(_ptr(y0), _ptr(y1), _ptr(ks), n, h, t_new, _ptr(ts),
                                        len(ts), _ptr(out)) == 0
     return out
+
+
+def ic_plummer(n: int, seed: int, a: float = 1.0) -> np.ndarray:
+    """Seeded Plummer sphere, the same bits as the library's gb_ic_plummer
+    (for the CPU-baseline legs, which must not load the GPU library)."""
+    x = np.zeros(6 * n)
+    assert lib().orc_ic_plummer(n, seed, a, _ptr(x)) == 0
+    return x
 
 
 def pi_sequence(safe: float, alpha: float, beta: float, minscale: float, maxscale: float,

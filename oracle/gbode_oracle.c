@@ -1174,3 +1174,98 @@ int orc_spinning_cube(int64_t n, double L, uint32_t seed, double* x_out) {
 size_t orc_sizeof_tableau(void) { return sizeof(orc_tableau); }
 size_t orc_sizeof_ode(void) { return sizeof(orc_ode); }
 size_t orc_sizeof_stats(void) { return sizeof(orc_stats); }
+
+/* ------------------------------------------------------------------------ */
+/* Seeded Plummer sphere for the CPU-baseline legs of the benchmark, so      */
+/* that they build their inputs without the GPU library: the same sampler   */
+/* as the library's initial conditions (Aarseth, Henon & Wielen 1974:       */
+/* r = a / sqrt(X^(-2/3) - 1) with X < 0.999, speed q sqrt(2) (1 + r^2 /    */
+/* a^2)^(-1/4) / sqrt(a) with g(q) = q^2 (1 - q^2)^(7/2) by rejection,      */
+/* isotropic directions, centre of mass removed), drawing from xoshiro256** */
+/* seeded through splitmix64 (Blackman & Vigna), uniform doubles from the   */
+/* top 53 bits.  The same seed gives the same bits as gb_ic_plummer.        */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  uint64_t s[4];
+} orc_rng;
+
+static uint64_t orc_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static void orc_rng_seed(orc_rng* g, uint64_t seed) {
+  uint64_t z = seed;
+  for (int i = 0; i < 4; ++i) {
+    z += 0x9e3779b97f4a7c15ULL;
+    uint64_t x = z;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
+    g->s[i] = x ^ (x >> 31);
+  }
+}
+
+static uint64_t orc_rng_next(orc_rng* g) {
+  uint64_t* s = g->s;
+  const uint64_t r = orc_rotl(s[1] * 5, 7) * 9;
+  const uint64_t t = s[1] << 17;
+  s[2] ^= s[0];
+  s[3] ^= s[1];
+  s[1] ^= s[2];
+  s[0] ^= s[3];
+  s[2] ^= t;
+  s[3] = orc_rotl(s[3], 45);
+  return r;
+}
+
+static double orc_uniform(orc_rng* g) {
+  return (double)(orc_rng_next(g) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static void orc_unit_vector(orc_rng* g, double* x, double* y, double* z) {
+  const double c = 2.0 * orc_uniform(g) - 1.0;
+  const double ph = 6.283185307179586 * orc_uniform(g);
+  const double s = sqrt(1.0 - c * c);
+  *x = s * cos(ph);
+  *y = s * sin(ph);
+  *z = c;
+}
+
+int orc_ic_plummer(int64_t n, uint64_t seed, double a, double* x) {
+  if (n < 2 || !x || !(a > 0.0)) return -1;
+  orc_rng g;
+  orc_rng_seed(&g, seed);
+  for (int64_t i = 0; i < n; ++i) {
+    double* p = x + 3 * i;
+    double* v = x + 3 * n + 3 * i;
+    double X;
+    do X = orc_uniform(&g);
+    while (X <= 0.0 || X >= 0.999);
+    const double r = a / sqrt(pow(X, -2.0 / 3.0) - 1.0);
+    double ux, uy, uz;
+    orc_unit_vector(&g, &ux, &uy, &uz);
+    p[0] = r * ux;
+    p[1] = r * uy;
+    p[2] = r * uz;
+    double q, y;
+    do {
+      q = orc_uniform(&g);
+      y = 0.1 * orc_uniform(&g);
+    } while (y > q * q * pow(1.0 - q * q, 3.5));
+    const double sp = q * sqrt(2.0) * pow(1.0 + r * r / (a * a), -0.25) / sqrt(a);
+    orc_unit_vector(&g, &ux, &uy, &uz);
+    v[0] = sp * ux;
+    v[1] = sp * uy;
+    v[2] = sp * uz;
+  }
+  double c[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) {
+      c[k] += x[3 * i + k];
+      c[3 + k] += x[3 * n + 3 * i + k];
+    }
+  for (int k = 0; k < 6; ++k) c[k] /= (double)n;
+  for (int64_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) {
+      x[3 * i + k] -= c[k];
+      x[3 * n + 3 * i + k] -= c[3 + k];
+    }
+  return 0;
+}

@@ -75,9 +75,19 @@ def test_matches_reference_runs(gb, torch_cuda, tag, exact):
     n = int(n)
     times, states, st = run(gb, str(d["tableau"]), n, soft, mass, d["x0"], t0, tf, tol,
                             exact=exact)
+    # the parity bar: the same accepted-step count and a final state within
+    # 10x the tolerance
     assert len(times) == len(d["times"]), (len(times), len(d["times"]))
     assert np.max(np.abs(states[-1] - d["final"])) <= 10 * tol
-    np.testing.assert_allclose(times, d["times"], rtol=0, atol=10 * tol)
+    if exact:
+        # the reference's arithmetic: its step times bit for bit
+        np.testing.assert_array_equal(times, d["times"])
+    else:
+        # FP64 stages with the refined-rsqrt pair term (a few ulp per term):
+        # the step sizes follow err^(-1/(1+q)) of a near-cancelling error
+        # estimate, so the accepted times drift from the reference's by
+        # ~1e-7 relative over a run
+        np.testing.assert_allclose(times, d["times"], rtol=1e-6, atol=10 * tol)
 
 
 @pytest.mark.parametrize("n,tab,seed", [(48, "DOPRI5", 1), (100, "RKF78", 2), (33, "RKF45", 3),
@@ -138,12 +148,36 @@ def test_element_epilogue_is_bit_identical(gb, torch_cuda, n, zero_mass):
         np.testing.assert_array_equal(s, s0, err_msg=str(key))
 
 
-def _mixed_run(gb, ode, x0, tf, tol, tile=None, variant=0):
+def _mixed_run(gb, ode, x0, tf, tol, tile=None, variant=0, spatial_sort=0, tab="DOPRI5",
+               attempts_per_sync=16):
     exe = gb.Gb300Executor(precision="mixed", tile=tile if tile is not None
-                           else gb.tiling(mixed_variant=variant))
+                           else gb.tiling(mixed_variant=variant), spatial_sort=spatial_sort,
+                           attempts_per_sync=attempts_per_sync)
     out = gb.RawOutput()
-    st = gb.RKEmbeddedParallel("DOPRI5").integrate(x0, 0.0, tf, tol, tol, ode, out, exe)
+    st = gb.RKEmbeddedParallel(tab).integrate(x0, 0.0, tf, tol, tol, ode, out, exe)
     return np.array(out.times()), np.array(out.states()), st
+
+
+@pytest.mark.parametrize("n,gen", [(16384, "plummer"), (8333, "cold"), (12000, "binary")])
+def test_split_stage_tile_culling_is_bit_identical(gb, torch_cuda, n, gen):
+    """The partner-chunk stage on Morton-sorted bodies skips the close-pair
+    test for half tiles whose boxes are far from the i-tile; the terms it adds
+    there are the ones the test would have kept, so whole RKF78 trajectories
+    with and without the culling (re-sorted every 4 attempts) agree bit for
+    bit, and both follow the FP64 integration to the mixed-precision bound."""
+    x0 = {"plummer": lambda: gb.ic_plummer(n, 5), "cold": lambda: gb.ic_cold_sphere(n, 6, 0.01),
+          "binary": lambda: gb.ic_binary_plummer(n, 7, 0.1, 1e-3, 1e-2)}[gen]()
+    soft, tol, tf = 0.005, 1e-9, 0.05
+    ode = gb.NBodyODE(n, soft, 1.0 / n)
+    a = _mixed_run(gb, ode, x0, tf, tol, tab="RKF78", attempts_per_sync=4)
+    b = _mixed_run(gb, ode, x0, tf, tol, tab="RKF78", attempts_per_sync=4, spatial_sort=2)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    out64 = gb.RawOutput()
+    gb.RKEmbeddedParallel("RKF78").integrate(x0, 0.0, tf, tol, tol, ode, out64,
+                                             gb.Gb300Executor(precision="f64"))
+    assert abs(len(a[0]) - len(out64.times())) <= 2
+    assert np.max(np.abs(a[1][-1] - np.array(out64.states()[-1]))) <= 1e-6
 
 
 @pytest.mark.parametrize("n", [8192, 8333])
@@ -173,7 +207,8 @@ def test_split_stage_is_deterministic_and_tracks_fp64(gb, torch_cuda, n):
     ref = np.array(out64.states()[-1])
     runs = {"split": a, "cluster": _mixed_run(gb, ode, x0, tf, tol, tile=gb.tiling(8, 2, 0)),
             "split5": _mixed_run(gb, ode, x0, tf, tol, tile=gb.tiling(5, 1, 0)),
-            "pairs2": _mixed_run(gb, ode, x0, tf, tol, variant=2)}
+            "pairs2": _mixed_run(gb, ode, x0, tf, tol, variant=2),
+            "unsorted": _mixed_run(gb, ode, x0, tf, tol, spatial_sort=3)}
     for name, (t, s, st) in runs.items():
         assert t[-1] == tf, name
         assert abs(len(t) - len(out64.times())) <= 2, name

@@ -227,3 +227,10 @@ def test_dense_session_on_the_exponential(orc):
     s2.run()
     np.testing.assert_allclose(s2.dense(), states[3:6], rtol=1e-15, atol=0)
     s2.close()
+
+
+def test_oracle_plummer_initial_conditions_match_library(orc, gb):
+    """The CPU-baseline legs build their inputs with the oracle's copy of the
+    seeded Plummer sampler; it gives the library's bits (host code only)."""
+    for n, seed in ((1024, 1), (16384, 101), (333, 7)):
+        np.testing.assert_array_equal(orc.ic_plummer(n, seed, 1.0), gb.ic_plummer(n, seed, 1.0))
