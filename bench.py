@@ -717,7 +717,7 @@ def run_other_workload(args):
             eps = 0.01 * 4.0 / np.cbrt(sizes)
             x0 = _batch_ics(gb, torch, sizes, 3000 + np.arange(512), "virial", eps)
             tab, tol, tf = "DOPRI5", 1e-9, 1.0
-            prop = "proposer_batch_dopri5_tol1e-9.bin"
+            prop = "proposer_plummer512_dopri5_tol1e-9.bin"
         else:
             # configuration 5, batched part: 64 binary-rich Plummer spheres of
             # N = 8192 (10 % of the bodies in bound pairs, semimajor axes

@@ -445,6 +445,22 @@ struct TileBox {
   float4 c;
 };
 
+// Box from FP32 extents [lo, hi] per axis: centre (x, y, z) and a radius (w)
+// rounded outwards (the half-diagonal rounded up, widened by 1e-5 relative
+// and by the rounding of the centre) so that it bounds the distance of every
+// point of the extents from the rounded centre.
+__device__ __forceinline__ float4 box_from_extents(float lx, float ly, float lz, float hx,
+                                                   float hy, float hz) {
+  float4 b;
+  b.x = 0.5f * (lx + hx);
+  b.y = 0.5f * (ly + hy);
+  b.z = 0.5f * (lz + hz);
+  const float ex = 0.5f * (hx - lx), ey = 0.5f * (hy - ly), ez = 0.5f * (hz - lz);
+  const float r = __fsqrt_ru(__fmaf_ru(ez, ez, __fmaf_ru(ey, ey, __fmul_ru(ex, ex))));
+  b.w = r * 1.00001f + 3.0e-7f * (fabsf(b.x) + fabsf(b.y) + fabsf(b.z));
+  return b;
+}
+
 // True when no pair of the i-tile (box I, every body within |h_i| / 8 <=
 // ti of the reference point's near-pair threshold) and the j-tile (box J)
 // can be a close pair of the packed loop (r^2 < (|h_i| / 8)^2): the boxes'
@@ -457,26 +473,46 @@ __device__ __forceinline__ bool tiles_far(float4 I, float ti, float4 J) {
   return __fmul_rn(d, 1.0f - 1e-5f) - I.w - J.w > __fmul_rn(ti, 1.0f + 1e-5f);
 }
 
+// Box of a warp's 32 bodies from their hi parts (warp shuffles; invalid lanes
+// excluded): centre and a radius rounded outwards so that it bounds every hi
+// point's distance from the rounded centre.  Every lane returns the box.
+__device__ __forceinline__ float4 warp_box(float hx, float hy, float hz, bool valid) {
+  float v[6];
+  v[0] = valid ? hx : 3.0e38f;
+  v[1] = valid ? hy : 3.0e38f;
+  v[2] = valid ? hz : 3.0e38f;
+  v[3] = valid ? -hx : 3.0e38f;
+  v[4] = valid ? -hy : 3.0e38f;
+  v[5] = valid ? -hz : 3.0e38f;
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+  return box_from_extents(v[0], v[1], v[2], -v[3], -v[4], -v[5]);
+}
+
 // PAIRS (one lane per body): part is read as float2[BI][3] and receives each
 // sum as its FP32 Kahan pair (s, -c), value s - c, with no FP64 arithmetic.
 // CULL (one lane and one body per thread, 128 threads, partner ranges that
-// start at multiples of 128): boxes[t] bounds the packed positions of bodies
-// [128 t, 128 t + 128) and ibox the CTA's own; every 128-partner half of a
-// tile that tiles_far separates from the i-tile runs the pair loop without
-// the close-pair test.  Its terms are the ones the test would have kept, so
-// the sums are bit for bit those of the loop with the test.
+// start at multiples of 64): boxes[t] bounds the packed positions of bodies
+// [64 t, 64 t + 64).  Every warp boxes its own 32 bodies, and each 64-partner
+// quarter of a tile whose box tiles_far separates from the warp's (cull != 0)
+// runs the pair loop without the close-pair test.  Its terms are the ones the
+// test would have kept, so the sums are bit for bit those of the loop with
+// the test.
 template <int T, int L, int NB = 1, bool PAIRS = false, bool CULL = false>
 __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict__ packed,
                                                    long long n, long long i0, long long jb,
                                                    long long je, float eps2, unsigned char* smem,
                                                    double (*part)[3],
                                                    const float4* __restrict__ boxes = nullptr,
-                                                   float4 ibox = float4{}) {
+                                                   int cull = 0) {
   static_assert(!CULL || (L == 1 && NB == 1 && T == 128), "culling: 128 one-body threads");
   constexpr int BG = T / L;  // body groups per CTA (NB bodies each)
   constexpr int JT = 2 * T;  // partners per tile
-  __shared__ int sh_far[2][2];   // far flags of the two 128-partner halves, per buffer
-  __shared__ float4 sh_ibox[2];  // i-tile box, near-pair bound of its bodies
+  // per warp: its box (centre, radius) and the near-pair bound of its bodies,
+  // as scalars
+  __shared__ float sh_wbox[T / 32][5];
   PartnerPair* recs = reinterpret_cast<PartnerPair*>(smem);  // two buffers of T records
   PackedBody* raw = reinterpret_cast<PackedBody*>(smem + 2 * sizeof(PartnerPair) * T);
   const int g = threadIdx.x / L;
@@ -500,6 +536,22 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     LY[q] = f2_pack(pb.lo.y, pb.lo.y);
     LZ[q] = f2_pack(pb.lo.z, pb.lo.z);
     near2[q] = near_threshold_bits(pb.hw.x, pb.hw.y, pb.hw.z);
+    if constexpr (CULL) {
+      const float4 wb = warp_box(pb.hw.x, pb.hw.y, pb.hw.z, i < n);
+      if ((threadIdx.x & 31) == 0) {
+        float* wbs = sh_wbox[threadIdx.x >> 5];
+        wbs[0] = wb.x;
+        wbs[1] = wb.y;
+        wbs[2] = wb.z;
+        wbs[3] = wb.w;
+        // |h_i| <= |c_w| + R_w for every body of the warp: the near-pair
+        // threshold |h_i| / 8 is at most that over 8
+        const float cw = __fsqrt_rn(__fmaf_rn(wb.z, wb.z, __fmaf_rn(wb.y, wb.y,
+                                                                     __fmul_rn(wb.x, wb.x))));
+        wbs[4] = __fmul_rn(cw + wb.w, 0.125f);
+      }
+      __syncwarp();
+    }
   }
   const f2_t E2 = f2_pack(eps2, eps2);
   float sx[NB], sy[NB], sz[NB], cx[NB], cy[NB], cz[NB];
@@ -523,25 +575,21 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     }
     cp_async_commit();
   };
-  if constexpr (CULL) {
-    if (threadIdx.x == 0) {
-      sh_ibox[0] = ibox;
-      // |h_i| <= |c_I| + R_I for every body of the tile: the near-pair
-      // threshold |h_i| / 8 is at most that over 8
-      const float ci = __fsqrt_rn(__fmaf_rn(ibox.z, ibox.z,
-                                            __fmaf_rn(ibox.y, ibox.y, __fmul_rn(ibox.x, ibox.x))));
-      sh_ibox[1].x = __fmul_rn(ci + ibox.w, 0.125f);
-    }
-    __syncthreads();
-  }
-  auto build = [&](long long j0, PartnerPair* out) {
+  // Builds the records of the tile at j0 and returns (in every lane) the
+  // warp's far mask of the tile's four 64-partner quarters.
+  auto build = [&](long long j0, PartnerPair* out) -> unsigned {
     const int cnt = (int)min((long long)JT, je - j0);
+    unsigned fm = 0;
     if constexpr (CULL) {
-      if (threadIdx.x < 2) {
-        const long long h0 = j0 + 128 * (long long)threadIdx.x;
-        sh_far[out == recs ? 0 : 1][threadIdx.x] =
-            h0 < je ? (int)tiles_far(sh_ibox[0], sh_ibox[1].x, boxes[h0 / 128]) : 0;
+      const int lane = threadIdx.x & 31;
+      const long long h0 = j0 + 64 * (long long)lane;
+      bool far = false;
+      if (cull && lane < 4 && h0 < je) {
+        const float* wbs = sh_wbox[threadIdx.x >> 5];
+        far = tiles_far(make_float4(wbs[0], wbs[1], wbs[2], wbs[3]), wbs[4],
+                        __ldg(boxes + h0 / 64));
       }
+      fm = __ballot_sync(0xffffffffu, far);
     }
     if ((int)threadIdx.x < (cnt + 1) / 2) {
       const PackedBody a = raw[2 * threadIdx.x];
@@ -558,11 +606,13 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
       r.yz = make_ulonglong2(f2_pack(a.lo.y, b.lo.y), f2_pack(a.lo.z, b.lo.z));
       out[threadIdx.x] = r;
     }
+    return fm;
   };
+  unsigned fm = 0, fm_next = 0;  // far quarters of the current / next tile
   if (jb < je) {
     issue(jb);
     cp_async_wait_all();
-    build(jb, recs);
+    fm = build(jb, recs);
     if (jb + JT < je) issue(jb + JT);
   }
   __syncthreads();
@@ -583,8 +633,8 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     for (int k0 = 0; k0 < kn; k0 += 32) {
       const int kc = min(32, kn - k0);
       if constexpr (CULL) {
-        // records [0, 64) hold partners of the first 128-body half
-        if (sh_far[buf][k0 >= 64 ? 1 : 0]) {
+        // records [32 q, 32 q + 32) hold the partners of quarter q
+        if ((fm >> (k0 >> 5)) & 1u) {
 #pragma unroll 4
           for (int u = 0; u < kc; ++u) {
             const int jj = k0 + u;
@@ -677,10 +727,11 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     }
     if (j0 + JT < je) {
       cp_async_wait_all();                 // this thread's copies of tile k + 1
-      build(j0 + JT, recs + (buf ^ 1) * T);
+      fm_next = build(j0 + JT, recs + (buf ^ 1) * T);
       if (j0 + 2 * JT < je) issue(j0 + 2 * JT);
     }
     __syncthreads();
+    fm = fm_next;
   }
   if constexpr (PAIRS) {
     static_assert(L == 1, "Kahan pairs out: one lane per body");

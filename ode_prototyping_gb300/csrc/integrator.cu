@@ -136,18 +136,18 @@ __global__ void __launch_bounds__(T, PACKED ? 7 * 128 / T : 5 * 128 / T)
   if (threadIdx.x == 0) P.partials[ci.itile * ci.size + ci.rank] = tile_sum;
 }
 
-// Box of a sorted tile's new packed positions, by the CTA that finishes the
-// tile: min / max of the hi parts over its cnt bodies (warp shuffles, then
-// the four warps in shared memory), centre and a radius rounded outwards so
-// that it bounds every hi point's distance from the rounded centre.  The load
-// (box_load, one body per thread) is issued early; box_write reduces and
-// writes.  All 128 threads must call box_write.
+// Boxes of a sorted tile's new packed positions, one per 64 bodies, by the
+// CTA that finishes the tile: min / max of the hi parts (warp shuffles, then
+// warp pairs in shared memory), centre and a radius rounded outwards
+// (box_from_extents).  The load (box_load, one body per thread) is issued
+// early; box_write reduces and writes out[0] (bodies 0..63) and out[1]
+// (64..127, when the tile has them).  All 128 threads must call box_write.
 __device__ __forceinline__ float4 box_load(const PackedBody* __restrict__ p, int cnt) {
   return (int)threadIdx.x < cnt ? __ldcg(&p[threadIdx.x].hw)
                                 : make_float4(nanf(""), 0.f, 0.f, 0.f);
 }
 
-__device__ __forceinline__ void box_write(float4 h, float4* out, float* red) {
+__device__ __forceinline__ void box_write(float4 h, int cnt, float4* out, float* red) {
   const bool valid = !isnan(h.x);
   float v[6];
   if (valid) {
@@ -166,36 +166,26 @@ __device__ __forceinline__ void box_write(float4 h, float4* out, float* red) {
 #pragma unroll
     for (int k = 0; k < 6; ++k) red[6 * w + k] = v[k];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    float lo[3], hi[3];
-    for (int k = 0; k < 3; ++k) {
-      lo[k] = fminf(fminf(red[k], red[6 + k]), fminf(red[12 + k], red[18 + k]));
-      hi[k] = -fminf(fminf(red[3 + k], red[9 + k]), fminf(red[15 + k], red[21 + k]));
-    }
-    float4 b;
-    b.x = 0.5f * (lo[0] + hi[0]);
-    b.y = 0.5f * (lo[1] + hi[1]);
-    b.z = 0.5f * (lo[2] + hi[2]);
-    const float ex = 0.5f * (hi[0] - lo[0]), ey = 0.5f * (hi[1] - lo[1]),
-                ez = 0.5f * (hi[2] - lo[2]);
-    const float r = __fsqrt_ru(__fmaf_ru(ez, ez, __fmaf_ru(ey, ey, __fmul_ru(ex, ex))));
-    b.w = r * 1.00001f + 3.0e-7f * (fabsf(b.x) + fabsf(b.y) + fabsf(b.z));
-    *out = b;
+  if (threadIdx.x < 2 && 64 * (int)threadIdx.x < cnt) {
+    const float* r0 = red + 12 * threadIdx.x;  // warps 2h and 2h + 1
+    out[threadIdx.x] = box_from_extents(fminf(r0[0], r0[6]), fminf(r0[1], r0[7]),
+                                        fminf(r0[2], r0[8]), -fminf(r0[3], r0[9]),
+                                        -fminf(r0[4], r0[10]), -fminf(r0[5], r0[11]));
   }
   __syncthreads();
 }
 
 __device__ __forceinline__ void write_tile_box(const PackedBody* __restrict__ p, int cnt,
                                                float4* out, float* red) {
-  box_write(box_load(p, cnt), out, red);
+  box_write(box_load(p, cnt), cnt, out, red);
 }
 
 // One CTA of 128 threads per tile: packs the positions of x0 (ring slot
-// *cur) in the order perm into out[*slot] and writes the tile boxes.
+// *cur) in the order perm into out[*slot] and writes the tile's two boxes.
 __global__ void __launch_bounds__(128)
     pack_boxes_kernel(const double* __restrict__ ring, const int* cur, long long n_var,
                       long long n, const int* __restrict__ perm, const double* __restrict__ cref,
-                      PackedBody* out, const int* slot, float4* boxes, long long n_tiles) {
+                      PackedBody* out, const int* slot, float4* boxes, long long n_boxes) {
   __shared__ float red[32];
   const double* x = ring + (long long)*cur * n_var;
   PackedBody* o = out + (long long)*slot * n;
@@ -208,7 +198,7 @@ __global__ void __launch_bounds__(128)
   }
   __threadfence_block();
   __syncthreads();
-  write_tile_box(o + i0, cnt, boxes + (long long)*slot * n_tiles + blockIdx.x, red);
+  write_tile_box(o + i0, cnt, boxes + (long long)*slot * n_boxes + 2 * blockIdx.x, red);
 }
 
 __global__ void iota_kernel(int* p, long long n) {
@@ -216,9 +206,8 @@ __global__ void iota_kernel(int* p, long long n) {
   if (i < n) p[i] = (int)i;
 }
 
-// Rows [rb, rb + cnt) of a sorted i-tile (bodies perm[i0 + rb ..]) before the
-// stage's pair loop: everything of the stage combination that does not need
-// this stage's accelerations.  The position elements are finished here (their
+// Rows [rb, rb + cnt) of a sorted i-tile (bodies perm[i0 + rb ..]): everything
+// of the stage combination that does not need this stage's accelerations.  The position elements are finished here (their
 // stage derivative is the stage state's velocity): k_s, the next stage state
 // (or, at the last stage, the candidate state, its error, target and scaled
 // square) and the packed hi/lo positions of the next stage at their sorted
@@ -250,8 +239,8 @@ __device__ __forceinline__ void split_pre_rows(const DevTableau& tab, const Fuse
       ks_now = ysrc[3 * n + idx];  // dx/dt = v of the stage state
       ks_s[idx] = ks_now;
     }
-    // every term's load in flight at once (this runs before the pair loop,
-    // whose registers are not live yet), then the sum in stage order
+    // every term's load in flight at once (this runs after the pair loop,
+    // whose registers are no longer live), then the sum in stage order
     double kl[GB_MAX_STAGES];
     if (!last) {
       const unsigned m = tab.anz[s];
@@ -316,16 +305,17 @@ __device__ __forceinline__ void split_pre_rows(const DevTableau& tab, const Fuse
 // CTAs to one (the warp schedulers favour older CTAs: identical CTAs finished
 // their pair loops between 45 and 128 us at N = 16384) while an 8-CTA cluster
 // waited for its slowest rank; independent CTAs let the block scheduler
-// refill every SM until the last chunks.  Each CTA first finishes its slice
-// of the tile's rows as far as this stage's accelerations allow
-// (split_pre_rows), then runs the pair loop, in which every 128-partner half
-// tile whose box is far from the i-tile's skips the close-pair test (sorted
-// tiles are compact, so most are), and stores its chunk's sums as FP32 Kahan
-// pairs.  The CTA whose arrival completes the tile's count (an atomic
-// increment; nothing waits) adds the chunks in chunk order, so the sums do
-// not depend on which CTA arrives last, resets the count for the next launch,
-// adds the last term of every velocity element and writes the box of the
-// tile's new positions for the next stage.
+// refill every SM until the last chunks.  Each CTA runs the pair loop, in
+// which every 64-partner quarter tile whose box is far from the box of a
+// warp's 32 bodies skips the close-pair test for that warp (sorted bodies are
+// compact, so many are), and stores its chunk's sums as FP32 Kahan pairs;
+// the CTAs of a middle band of chunks then finish a slice of the tile's rows
+// as far as this stage's accelerations allow (split_pre_rows).  The CTA whose
+// arrival completes the tile's count (an atomic increment; nothing waits)
+// adds the chunks in chunk order, so the sums do not depend on which CTA
+// arrives last, resets the count for the next launch, adds the last term of
+// every velocity element and writes the boxes of the tile's new positions for
+// the next stage.
 template <int T, int L, int BPT>
 __global__ void __launch_bounds__(T, 7 * 128 / T)
     fused_split_kernel(const __grid_constant__ DevTableau tab,
@@ -336,6 +326,7 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
   __shared__ __align__(16) unsigned char sh_raw[jp_smem_bytes<T>()];
   __shared__ double part[BI][3];
   __shared__ double red[T];
+  __shared__ double sh_pos[3 * BI];
   __shared__ int sh_last;
   Ctrl* C = P.ctrl;
   if (C->done) return;
@@ -351,8 +342,9 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
   const bool skip_force = (s == 0 && C->k0_valid);
   const int b_hi = (int)min((long long)BI, n - i0);
   PackedBody* pnext = last ? P.PX + (long long)(C->px ^ 1) * n : P.PY + (long long)((s + 1) & 1) * n;
-  float4* box_next = last ? P.BX + (long long)(C->px ^ 1) * P.n_itiles
-                          : P.BY + (long long)((s + 1) & 1) * P.n_itiles;
+  // boxes: two per tile (64 bodies each) per buffer
+  float4* box_next = last ? P.BX + (long long)(C->px ^ 1) * 2 * P.n_itiles
+                          : P.BY + (long long)((s + 1) & 1) * 2 * P.n_itiles;
   if (skip_force) {
     // the stage derivative is reused: one CTA per tile runs the whole epilogue
     if (chunk != 0) return;
@@ -393,37 +385,41 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
     }
     __threadfence_block();
     __syncthreads();
-    write_tile_box(pnext + i0, b_hi, box_next + itile, reinterpret_cast<float*>(red));
+    write_tile_box(pnext + i0, b_hi, box_next + 2 * itile, reinterpret_cast<float*>(red));
     return;
-  }
-  {
-    // this chunk's slice of the tile's rows, before the pair loop
-    const int rpc = (BI + nc - 1) / nc;
-    const int rb = chunk * rpc;
-    const int cnt = max(0, min(b_hi, rb + rpc) - rb);
-    double sq_pos = 0.0;
-    split_pre_rows<T>(tab, P, C, s, i0, rb, cnt, &part[0][0], sq_pos);
-    if (last) {
-      const double v = block_sum(sq_pos, red);
-      if (threadIdx.x == 0) P.partials[itile * (nc + 1) + chunk] = v;
-    }
-    __syncthreads();  // part (the slice's positions) is free for the pair sums
   }
   const long long jb = P.chunk_start[chunk], je = P.chunk_start[chunk + 1];
   const PackedBody* src = (s == 0) ? P.PX + (long long)C->px * n : P.PY + (long long)(s & 1) * n;
-  const float4* boxes = (s == 0) ? P.BX + (long long)C->px * P.n_itiles
-                                 : P.BY + (long long)(s & 1) * P.n_itiles;
-  if (P.cull) {
-    force_mixed_cta_jp<T, L, BPT, true, true>(src, n, i0, jb, je, P.eps2f, sh_raw, part, boxes,
-                                              boxes[itile]);
-  } else {
-    force_mixed_cta_jp<T, L, BPT, true>(src, n, i0, jb, je, P.eps2f, sh_raw, part);
-  }
+  const float4* boxes = (s == 0) ? P.BX + (long long)C->px * 2 * P.n_itiles
+                                 : P.BY + (long long)(s & 1) * 2 * P.n_itiles;
+  force_mixed_cta_jp<T, L, BPT, true, true>(src, n, i0, jb, je, P.eps2f, sh_raw, part, boxes,
+                                            P.cull);
   __syncthreads();
   // the chunk's sums leave as FP32 Kahan pairs (s, -c)
   const float2* pf = reinterpret_cast<const float2*>(&part[0][0]);
   float2* mine = reinterpret_cast<float2*>(P.chunk_sums) + (itile * nc + chunk) * BW;
   for (int e = threadIdx.x; e < BW; e += T) mine[e] = pf[e];
+  // The CTAs of chunks [nc/2, nc/2 + npre) finish the tile's rows as far as
+  // this stage's accelerations allow, one slice each, after their pair loops:
+  // not in the first wave of the launch (it would hold every SM's FMA pipes
+  // idle while its FP64 loads return), not in the last chunks (their CTAs end
+  // the launch).  At the last stage every chunk's slot of the partial sums is
+  // written (zero outside those CTAs).
+  {
+    const int c0 = nc / 2, npre = max(1, nc / 4);
+    const int slice = chunk - c0;
+    double sq_pos = 0.0;
+    if (slice >= 0 && slice < npre) {
+      const int rpc = (BI + npre - 1) / npre;
+      const int rb = slice * rpc;
+      const int cnt = max(0, min(b_hi, rb + rpc) - rb);
+      split_pre_rows<T>(tab, P, C, s, i0, rb, cnt, sh_pos, sq_pos);
+    }
+    if (last) {
+      const double v = block_sum(sq_pos, red);
+      if (threadIdx.x == 0) P.partials[itile * (nc + 1) + chunk] = v;
+    }
+  }
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) sh_last = atomicAdd(P.tile_count + itile, 1u) == (unsigned)(nc - 1);
@@ -508,7 +504,7 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
       sq_acc = dadd(sq_acc, dmul(q, q));
     }
   }
-  box_write(bx, box_next + itile, reinterpret_cast<float*>(red));
+  box_write(bx, b_hi, box_next + 2 * itile, reinterpret_cast<float*>(red));
   if (!last) return;
   double amax = 0.0;
   for (int b = threadIdx.x; b < b_hi; b += T) {
@@ -1117,7 +1113,7 @@ int launch_resort(gb_integrator_s* it) {
     }
     pack_boxes_kernel<<<(unsigned)it->geom.n_itiles, 128, 0, s>>>(
         it->ring, cur, it->n_var, it->n, it->perm, it->cref, it->PX, px, it->BX,
-        it->geom.n_itiles);
+        2 * it->geom.n_itiles);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
   }
@@ -1304,8 +1300,8 @@ extern "C" int gb_integrator_create(const gb_tableau* tab, const gb_nbody_system
     GB_ALLOC(it->tile_count, (size_t)it->geom.n_itiles * sizeof(unsigned));
     e = cudaMemset(it->tile_count, 0, (size_t)it->geom.n_itiles * sizeof(unsigned));
     GB_ALLOC(it->pre, (size_t)nv * sizeof(double));
-    GB_ALLOC(it->BX, (size_t)2 * it->geom.n_itiles * sizeof(float4));
-    GB_ALLOC(it->BY, (size_t)2 * it->geom.n_itiles * sizeof(float4));
+    GB_ALLOC(it->BX, (size_t)4 * it->geom.n_itiles * sizeof(float4));  // 2 buffers x 2 per tile
+    GB_ALLOC(it->BY, (size_t)4 * it->geom.n_itiles * sizeof(float4));
     GB_ALLOC(it->perm, (size_t)n * sizeof(int));
     if (e == cudaSuccess) {
       iota_kernel<<<(unsigned)((n + 255) / 256), 256>>>(it->perm, n);

@@ -231,6 +231,11 @@ CONFIGS = {
     # over t in [0, 2] is below 1e-8
     "plummer16384_rkf78_tol1e-11": dict(ic="plummer", n=16384, softening=0.005, tab="RKF78",
                                         tol=1e-11, tf=2.0, attempts=800),
+    # configuration 3's integrator on one of its mid-size members: Plummer
+    # N = 512, eps = 0.01 * 4 / 512^(1/3) = 0.005, DOPRI5, tol 1e-9, t in [0, 1]
+    # (the proposer the batched C3 workload runs)
+    "plummer512_dopri5_tol1e-9": dict(ic="plummer", n=512, softening=0.005, tab="DOPRI5",
+                                      tol=1e-9, tf=1.0, attempts=600),
 }
 SEEDS_A = list(range(1, 17))
 SEEDS_B = list(range(101, 117))
