@@ -74,7 +74,7 @@ FLOPS_PER_INTERACTION = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) conven
 HILO_FP32_OPS = 11.5
 # DRAM bytes (read + write) of one headline stage launch from an ncu capture
 # of the same kernel and geometry (python bench.py --workload stage).
-STAGE_DRAM_BYTES_16384 = 2542592
+STAGE_DRAM_BYTES_16384 = 2722816
 FP64_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (non-tensor), one FMA = 2 FLOP
 
 
@@ -408,8 +408,8 @@ def main():
     ap.add_argument("--learned-config", default="plummer4096_rkf78",
                     help="c4: proposer training/evaluation configuration")
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c2_f64", "c2_tol", "c1", "c3", "c4", "c5a", "c5b", "rk_hbm",
-                             "stage"],
+                    choices=["c2", "c2_f64", "c2_tol", "c2_sweep", "c1", "c3", "c4", "c5a", "c5b",
+                             "rk_hbm", "stage"],
                     help="c2 (default, the headline), or another configuration")
     args = ap.parse_args()
     world, rank, local = dist_setup()
@@ -677,6 +677,49 @@ def run_other_workload(args):
                     config={**W, "atol": args.tol, "rtol": args.tol,
                             "workload": "plummer16384_rkf78_tight_tolerance",
                             "step": "one whole integration per path"})
+    elif args.workload == "c2_sweep":
+        # The controllers compared at equal energy error: the headline system
+        # integrated t = 0 -> 2 (mixed precision) by the reference, PI and
+        # learned controllers, each at the tolerances 3e-12, 1e-11, 3e-11; for
+        # each controller the time to tf at a common relative energy error
+        # (the geometric mean of the three controllers' errors at 1e-11) is
+        # read off its own sweep by log-log interpolation in the tolerance.
+        W = WORKLOAD
+        n, eps = W["n_particles"], W["softening"]
+        x0 = gb.to_device(gb.ic_plummer(n, W["seed"], 1.0))
+        e0 = gb.energy(x0, n, eps, 1.0 / n)
+        mlp = load_mlp()
+        tols = [3e-12, 1e-11, 3e-11]
+        sweep = {}
+        for ctl in ("reference", "pi", "learned"):
+            integrate_once(gb, torch, x0, stream, "mixed", ctl, 1e-11, mlp)  # warm-up
+            rows = []
+            for tol in tols:
+                ms, st, xs = integrate_once(gb, torch, x0, stream, "mixed", ctl, tol, mlp)
+                rows.append({"tol": tol, **arm_record(gb, x0, e0, ms, st, xs)})
+            sweep[ctl] = rows
+        target = float(np.exp(np.mean([np.log(sweep[c][1]["energy_rel_err"]) for c in sweep])))
+
+        def at_target(rows):
+            le = np.log([r["energy_rel_err"] for r in rows])
+            lt = np.log([r["time_to_tf_s"] for r in rows])
+            lr = np.log([r["rhs_evals"] for r in rows])
+            order = np.argsort(le)
+            le, lt, lr = le[order], lt[order], lr[order]
+            x = np.log(target)
+            return {"time_to_tf_s": float(np.exp(np.interp(x, le, lt))),
+                    "rhs_evals": float(np.exp(np.interp(x, le, lr))),
+                    "inside_sweep": bool(le[0] <= x <= le[-1])}
+        eq = {c: at_target(sweep[c]) for c in sweep}
+        for c in ("reference", "pi"):
+            eq[f"learned_time_gain_vs_{c}"] = 1 - eq["learned"]["time_to_tf_s"] / eq[c]["time_to_tf_s"]
+            eq[f"learned_rhs_saved_vs_{c}"] = 1 - eq["learned"]["rhs_evals"] / eq[c]["rhs_evals"]
+        line.update(value=eq["learned"]["time_to_tf_s"], unit="s", higher_is_better=False,
+                    metric="time to tf at equal relative energy error (learned / PI / reference)",
+                    dtype="f32+f64", steps=1, ms_per_step=1e3 * eq["learned"]["time_to_tf_s"],
+                    energy_target=target, sweep=sweep, at_equal_energy=eq,
+                    config={**W, "tols": tols, "proposer": PROPOSER,
+                            "step": "whole integrations, three tolerances per controller"})
     elif args.workload == "c1":
         n, eps, tol = 1024, 0.01, 1e-10
         x0 = gb.to_device(gb.ic_uniform_ball(n, 1, 0.1))
@@ -705,10 +748,10 @@ def run_other_workload(args):
                             "step": "whole integration"})
         it.close()
     elif args.workload in ("c3", "c5b"):
-        # Batched ensembles, every arm over the whole [0, tf] of every system:
-        # mixed with the reference controller, mixed with the learned
-        # proposer (PI fallback), and the plain FP64 path; per-system relative
-        # energy errors at tf (max and median) beside the throughput.
+        # Batched ensembles: mixed with the reference controller and with the
+        # learned proposer (PI fallback) over the whole span, and all three
+        # arms (the plain FP64 path too) over a common window; per-system
+        # relative energy errors (max and median) beside the throughput.
         if args.workload == "c3":
             # configuration 3: 512 Plummer spheres, N log-uniform in [64, 4096],
             # virial ratio U(0.5, 1.5), eps = 0.01 * 4 / N^(1/3), DOPRI5, tol 1e-9
@@ -717,18 +760,19 @@ def run_other_workload(args):
             eps = 0.01 * 4.0 / np.cbrt(sizes)
             x0 = _batch_ics(gb, torch, sizes, 3000 + np.arange(512), "virial", eps)
             tab, tol, tf = "DOPRI5", 1e-9, 1.0
-            prop = "proposer_plummer512_dopri5_tol1e-9.bin"
+            prop = "proposer_batch3_dopri5_tol1e-9.bin"
         else:
             # configuration 5, batched part: 64 binary-rich Plummer spheres of
             # N = 8192 (10 % of the bodies in bound pairs, semimajor axes
             # log-uniform in [1e-3, 1e-2]); the configuration gives no
             # softening, the pairs need one well below their separations:
-            # eps = 1e-4; DOPRI5, tol 1e-8, t in [0, 5e-4] (the FP64 arm takes
-            # about two minutes over it)
+            # eps = 1e-4; DOPRI5, tol 1e-8, t in [0, 0.02] (about one and a
+            # half periods of the tightest pairs; the FP64 arm takes under a
+            # minute over it)
             sizes = np.full(64, 8192, dtype=np.int64)
             eps = np.full(64, 1e-4)
             x0 = _batch_ics(gb, torch, sizes, 6000 + np.arange(64), "binary", eps)
-            tab, tol, tf = "DOPRI5", 1e-8, 5e-4
+            tab, tol, tf = "DOPRI5", 1e-8, 0.02
             prop = "proposer_binary2048_dopri5.bin"
         x0d = gb.to_device(x0)
         offs = np.concatenate([[0], np.cumsum(sizes)]) * 6
@@ -737,25 +781,27 @@ def run_other_workload(args):
         ppath = os.path.join(ROOT, "ode_prototyping_gb300", "weights", prop)
         mlp = (gb.GbMlp.from_buffer_copy(open(ppath, "rb").read())
                if os.path.exists(ppath) else None)
-        res = {}
-        arms = [("mixed", "mixed", "reference"), ("f64", "f64", "reference")]
-        if mlp is not None:
-            arms.insert(1, ("learned_mixed", "mixed", "learned"))
-        for key, prec, ctl in arms:
+        # The plain FP64 batch over the whole span would take many minutes
+        # (about 100x the mixed batch), so every arm is also integrated over
+        # a common window [0, t_w] at the same tolerance: throughput and
+        # per-system energy errors there, FP64 included; the mixed arms
+        # additionally over the whole [0, tf].
+        t_w = tf / 20 if args.workload == "c3" else tf
+
+        def run_arm(prec, ctl, t_end, reps):
             b = gb.Batch(tab, sizes, eps, precision=prec, controller=ctl, attempts_per_sync=8,
-                         stream=stream, mlp=mlp if ctl == "learned" else None)
-            b.start(x0d, 0.0, tf, tol, tol)
+                         stream=stream, mlp=mlp if ctl == "learned" else None,
+                         max_attempts=200000)
+            b.start(x0d, 0.0, t_end, tol, tol)
             tune = b.autotune(2)
 
             def job():
-                b.start(x0d, 0.0, tf, tol, tol)
+                b.start(x0d, 0.0, t_end, tol, tol)
                 rc = b.advance(0)
                 assert rc == 0, rc
                 return b.stats()
-            reps = args.steps if prec == "mixed" else 1
-            if prec == "mixed":
-                for _ in range(args.warmup):
-                    job()
+            if reps > 1:
+                job()  # warm-up
             ms, st = _timed(torch, stream, job, reps, flush)
             xs, ts = b.state()
             errs = []
@@ -765,31 +811,37 @@ def run_other_workload(args):
                 errs.append(abs(e1["e"] - e0[k]["e"]) / abs(e0[k]["e"]))
             acc = sum(s["n_accepted"] for s in st)
             inter = sum(s["interactions"] for s in st)
-            res[key] = {"accepted_steps_per_s": acc / (ms / 1e3),
-                        "pair_interactions_per_s": inter / (ms / 1e3),
-                        "time_to_tf_s": ms / len(st) / 1e3, "geometry": tune,
-                        "accepted": st[0]["n_accepted"], "attempts": st[0]["n_attempts"],
-                        "rhs_evals": st[0]["n_rhs"], "t_min": float(ts.min()),
-                        "energy_rel_err_max": float(np.max(errs)),
-                        "energy_rel_err_median": float(np.median(errs))}
             b.close()
-        f64 = res["f64"]
-        for key in res:
-            if key != "f64":
-                res[f"speedup_time_to_tf_{key}_vs_f64"] = (f64["time_to_tf_s"]
-                                                           / res[key]["time_to_tf_s"])
-        head = res["learned_mixed"] if "learned_mixed" in res else res["mixed"]
+            r = {"t_end": t_end, "accepted_steps_per_s": acc / (ms / 1e3),
+                 "pair_interactions_per_s": inter / (ms / 1e3),
+                 "time_s": ms / len(st) / 1e3, "geometry": tune,
+                 "accepted": st[0]["n_accepted"], "attempts": st[0]["n_attempts"],
+                 "rhs_evals": st[0]["n_rhs"], "t_min": float(ts.min()),
+                 "energy_rel_err_max": float(np.max(errs)),
+                 "energy_rel_err_median": float(np.median(errs))}
+            print(json.dumps({"arm": [prec, ctl, t_end], **r}), flush=True)
+            return r
+        ctls = ["reference"] + (["learned"] if mlp is not None else [])
+        full = {f"mixed_{c}": run_arm("mixed", c, tf, args.steps) for c in ctls}
+        window = {f"mixed_{c}": run_arm("mixed", c, t_w, args.steps) for c in ctls}
+        window["f64_reference"] = run_arm("f64", "reference", t_w, 1)
+        f64 = window["f64_reference"]
+        for key in list(window):
+            if key != "f64_reference":
+                window[f"speedup_time_{key}_vs_f64"] = f64["time_s"] / window[key]["time_s"]
+        head = full.get("mixed_learned", full["mixed_reference"])
         line.update(value=head["accepted_steps_per_s"], dtype="f32+f64",
-                    steps=args.steps, ms_per_step=1e3 * head["time_to_tf_s"],
-                    pair_interactions_per_s=head["pair_interactions_per_s"], arms=res,
+                    steps=args.steps, ms_per_step=1e3 * head["time_s"],
+                    pair_interactions_per_s=head["pair_interactions_per_s"],
+                    whole_span=full, window=window,
                     config={"workload": args.workload, "systems": int(len(sizes)),
                             "n_min": int(sizes.min()), "n_max": int(sizes.max()),
                             "bodies": int(sizes.sum()), "tableau": tab, "atol": tol,
-                            "rtol": tol, "t": [0, tf],
+                            "rtol": tol, "t": [0, tf], "t_window": [0, t_w],
                             "softening": "0.01 * 4 / N^(1/3)" if args.workload == "c3"
                             else float(eps[0]),
                             "proposer": prop if mlp is not None else None,
-                            "step": "whole batch integration, every system to tf"})
+                            "step": "whole batch integration, every system to t_end"})
     elif args.workload == "stage":
         # Four stage launches of the headline integrator on an N-body Plummer
         # sphere (a small case for profiling the fused stage kernel).
@@ -799,6 +851,12 @@ def run_other_workload(args):
                            gb.Gb300Executor(precision=args.stage_precision, attempts_per_sync=1),
                            stream=stream)
         it.start(x0, WORKLOAD["t0"], WORKLOAD["tf"], WORKLOAD["atol"], WORKLOAD["rtol"])
+        # one whole attempt first (13 launches), so every stage buffer and
+        # tile box holds the integration's own data
+        with torch.cuda.stream(stream):
+            for r in range(gb.tableau(WORKLOAD["tableau"]).n_stages):
+                it.launch_stage(r)
+        stream.synchronize()
         ms, _ = _timed(torch, stream, lambda: it.launch_stage(1), 1, flush)
         with torch.cuda.stream(stream):
             for r in range(3):
@@ -810,7 +868,8 @@ def run_other_workload(args):
                     geometry=it.geometry(),
                     config={"workload": f"plummer{n}_rkf78_{args.stage_precision}_stage",
                             "n_particles": n,
-                            "step": "one fused stage launch (four launched)"})
+                            "step": "one fused stage launch (a whole attempt of 13, then "
+                                    "four more launched)"})
         it.close()
     elif args.workload == "c4":
         # Learned step-size proposer: trained on seed set A (weights shipped in

@@ -10,6 +10,13 @@ namespace gb {
 
 constexpr double kMaxStepScale = 6.0;   // RKEmbeddedParallel.hpp:21
 constexpr double kMinStepScale = 0.33;  // RKEmbeddedParallel.hpp:22
+// The learned proposal is a correction of at most this log factor (x3 either
+// way) to the PI controller's log step ratio.  Without the bound, a proposer
+// fed states outside its training distribution can keep shrinking steps that
+// the error estimate keeps accepting (measured: a configuration-3 batch ran
+// into its attempt budget), since acceptance only guards against steps that
+// are too long.
+constexpr double kLearnedMaxLogCorrection = 1.0986122886681098;  // log(3)
 
 // The reference's elementary controller (RKEmbeddedParallel.hpp:65-74):
 // dtnew = dt * safety / err^(1/(1+q)), clamped to x6 / x0.33, with a floor
@@ -135,7 +142,9 @@ __device__ inline void finish_attempt(const DevTableau& tab, const CtrlEnv& P, C
       const double base = err > 0.0 ? log(c.safety) - c.pi_alpha * log(err) +
                                           c.pi_beta * log(c.err_prev)
                                     : log(kMaxStepScale);
-      const double lg = fmin(fmax(base + learned_log_scale, log(kMinStepScale)),
+      const double res = fmin(fmax(learned_log_scale, -kLearnedMaxLogCorrection),
+                              kLearnedMaxLogCorrection);
+      const double lg = fmin(fmax(base + res, log(kMinStepScale)),
                              log(kMaxStepScale));
       double scale = exp(lg);
       if (c.reject_prev) scale = fmin(scale, 1.0);

@@ -317,7 +317,7 @@ __device__ __forceinline__ void split_pre_rows(const DevTableau& tab, const Fuse
 // every velocity element and writes the boxes of the tile's new positions for
 // the next stage.
 template <int T, int L, int BPT>
-__global__ void __launch_bounds__(T, 7 * 128 / T)
+__global__ void __launch_bounds__(T, 6 * 128 / T)
     fused_split_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ FusedParams P, int s) {
   static_assert(L == 1 && BPT == 1 && T == 128, "partner chunks: 128 one-body threads");
@@ -399,14 +399,15 @@ __global__ void __launch_bounds__(T, 7 * 128 / T)
   const float2* pf = reinterpret_cast<const float2*>(&part[0][0]);
   float2* mine = reinterpret_cast<float2*>(P.chunk_sums) + (itile * nc + chunk) * BW;
   for (int e = threadIdx.x; e < BW; e += T) mine[e] = pf[e];
-  // The CTAs of chunks [nc/2, nc/2 + npre) finish the tile's rows as far as
-  // this stage's accelerations allow, one slice each, after their pair loops:
-  // not in the first wave of the launch (it would hold every SM's FMA pipes
+  // The CTAs of chunks [nc/4, nc/2) finish the tile's rows as far as this
+  // stage's accelerations allow, one slice each, after their pair loops: not
+  // before the pair loop of the first wave (it would hold every SM's FMA pipes
   // idle while its FP64 loads return), not in the last chunks (their CTAs end
   // the launch).  At the last stage every chunk's slot of the partial sums is
-  // written (zero outside those CTAs).
+  // written (zero outside those CTAs).  Measured at N = 16384 (RKF78 stage):
+  // slices in chunks [nc/4, nc/2) 0.1316 ms, in [nc/2, 3nc/4) 0.1361 ms.
   {
-    const int c0 = nc / 2, npre = max(1, nc / 4);
+    const int c0 = nc / 4, npre = max(1, nc / 4);
     const int slice = chunk - c0;
     double sq_pos = 0.0;
     if (slice >= 0 && slice < npre) {

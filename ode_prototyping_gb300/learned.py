@@ -35,23 +35,39 @@ FEAT, LOG_DT, LOG_ERR, ACCEPTED = slice(0, 16), 16, 17, 18
 
 def initial_state(kind: str, n: int, seed: int) -> np.ndarray:
     """'plummer': Plummer sphere; 'binary': Plummer sphere with 10% of the
-    bodies in bound pairs, semimajor axes log-uniform in [1e-3, 1e-2]."""
+    bodies in bound pairs, semimajor axes log-uniform in [1e-3, 1e-2];
+    'virial': Plummer sphere with its velocities scaled by sqrt(Q), Q drawn
+    uniform in [0.5, 1.5) from the seed (configuration 3's members)."""
     if kind == "plummer":
         return ic_plummer(n, seed)
     if kind == "binary":
         return ic_binary_plummer(n, seed, 0.1, 1e-3, 1e-2)
+    if kind == "virial":
+        x = ic_plummer(n, seed)
+        x[3 * n:] *= np.sqrt(0.5 + np.random.default_rng(seed).uniform())
+        return x
     raise ValueError(f"unknown initial state {kind!r}")
+
+
+def member(n, softening, i: int):
+    """(bodies, softening) of the i-th training or evaluation run: a config's
+    n may be a list (runs cycle through it) and its softening the rule
+    'c3' (0.01 * 4 / N^(1/3), configuration 3's)."""
+    nn = n[i % len(n)] if isinstance(n, (list, tuple)) else n
+    soft = 0.04 / nn ** (1.0 / 3.0) if softening == "c3" else softening
+    return int(nn), float(soft)
 
 
 def collect_logs(seeds, n: int, softening: float, tab: str, tol: float, tf: float,
                  attempts: int, precision: str = "mixed", controller: str = "reference",
                  mlp: GbMlp | None = None, ic: str = "plummer"):
     logs = []
-    for seed in seeds:
-        x0 = initial_state(ic, n, seed)
+    for i, seed in enumerate(seeds):
+        nn, soft = member(n, softening, i)
+        x0 = initial_state(ic, nn, seed)
         exe = Gb300Executor(precision=precision, controller=controller, attempts_per_sync=16,
                             log_steps=attempts, mlp=mlp)
-        it = Integrator(tab, NBodyODE(n, softening, 1.0 / n), exe)
+        it = Integrator(tab, NBodyODE(nn, soft, 1.0 / nn), exe)
         it.start(x0, 0.0, tf, tol, tol)
         it.advance(attempts)
         logs.append(it.log())
@@ -202,8 +218,9 @@ def run_window(n: int, softening: float, tab: str, tol: float, t_end: float, see
 def evaluate(n, softening, tab, tol, t_end, seeds, mlp, precision="mixed", ic="plummer"):
     out = {}
     for ctl in ("reference", "pi", "learned"):
-        rows = [run_window(n, softening, tab, tol, t_end, s, ctl,
-                           mlp if ctl == "learned" else None, precision, ic) for s in seeds]
+        rows = [run_window(*member(n, softening, i), tab, tol, t_end, s, ctl,
+                           mlp if ctl == "learned" else None, precision, ic)
+                for i, s in enumerate(seeds)]
         agg = {k: float(np.sum([r[k] for r in rows])) for k in
                ("wall_s", "accepted", "rejected", "attempts", "rhs", "learned_proposals",
                 "learned_rejected")}
@@ -233,9 +250,15 @@ CONFIGS = {
                                         tol=1e-11, tf=2.0, attempts=800),
     # configuration 3's integrator on one of its mid-size members: Plummer
     # N = 512, eps = 0.01 * 4 / 512^(1/3) = 0.005, DOPRI5, tol 1e-9, t in [0, 1]
-    # (the proposer the batched C3 workload runs)
+    # (one size only: on the batch it took many more steps than the reference
+    # controller, hence the multi-size configuration below)
     "plummer512_dopri5_tol1e-9": dict(ic="plummer", n=512, softening=0.005, tab="DOPRI5",
                                       tol=1e-9, tf=1.0, attempts=600),
+    # configuration 3's members: Plummer spheres with virial ratio in [0.5, 1.5),
+    # N cycling through 64 .. 4096 (log-spaced), eps = 0.01 * 4 / N^(1/3),
+    # DOPRI5, tol 1e-9, t in [0, 1] (the proposer the batched C3 workload runs)
+    "batch3_dopri5_tol1e-9": dict(ic="virial", n=[64, 128, 256, 512, 1024, 2048, 4096, 181],
+                                  softening="c3", tab="DOPRI5", tol=1e-9, tf=1.0, attempts=800),
 }
 SEEDS_A = list(range(1, 17))
 SEEDS_B = list(range(101, 117))
