@@ -393,7 +393,9 @@ int gb_integrate_nbody(const gb_tableau* tab, const gb_nbody_system* sys,
 /* step size, decision and status.  No counterpart in the reference (its   */
 /* state size is a compile-time constant, src/state/ODEState.hpp:7-23).    */
 /* Work units (system, i-tile) are ordered by cost and taken round-robin by */
-/* a persistent stage kernel; one warp per system runs its controller; an  */
+/* a persistent stage kernel (small systems can share a CTA, one warp      */
+/* group each: gb_batch_tiling.systems_per_cta); one warp per system runs  */
+/* its controller; an                                                      */
 /* attempt is one CUDA graph replay.  Equal masses per system; scalar      */
 /* tolerances per system.  States are concatenated: system k occupies      */
 /* x[6*B_k .. 6*(B_k+N_k)) with B_k = N_0 + ... + N_{k-1}.                  */
@@ -405,6 +407,10 @@ typedef struct {
                                 f32x2 loop over pairs of partners at threads_per_cta <= 128,
                                 the scalar FP32 loop at 256 (0 = 1) */
   int32_t grid_ctas;         /* persistent grid (0 = 8 CTAs per SM) */
+  int32_t systems_per_cta;   /* 1, 2 or 4 (0 = 1): with G > 1, every system whose bodies fit
+                                one warp group's tile (N <= bodies per CTA tile / G) is
+                                integrated by a group of threads_per_cta / G threads, and
+                                G such systems share a CTA; larger systems take whole CTAs */
 } gb_batch_tiling;
 
 typedef struct {

@@ -84,7 +84,8 @@ class GbMlp(C.Structure):
 
 class GbBatchTiling(C.Structure):
     _fields_ = [("threads_per_cta", C.c_int32), ("lanes", C.c_int32),
-                ("bodies_per_thread", C.c_int32), ("grid_ctas", C.c_int32)]
+                ("bodies_per_thread", C.c_int32), ("grid_ctas", C.c_int32),
+                ("systems_per_cta", C.c_int32)]
 
 
 class GbBatchOpts(C.Structure):
@@ -727,7 +728,7 @@ class Batch:
         check(lib().gb_batch_autotune(self.h, reps, C.byref(t), C.byref(ms)), "gb_batch_autotune")
         return {"threads_per_cta": t.threads_per_cta, "lanes": t.lanes,
                 "bodies_per_thread": t.bodies_per_thread, "grid_ctas": t.grid_ctas,
-                "stage_ms": ms.value}
+                "systems_per_cta": t.systems_per_cta, "stage_ms": ms.value}
 
     def geometry(self) -> dict:
         t = GbBatchTiling()
@@ -735,7 +736,7 @@ class Batch:
         check(lib().gb_batch_geometry(self.h, C.byref(t), C.byref(nu)), "gb_batch_geometry")
         return {"threads_per_cta": t.threads_per_cta, "lanes": t.lanes,
                 "bodies_per_thread": t.bodies_per_thread, "grid_ctas": t.grid_ctas,
-                "units": int(nu.value)}
+                "systems_per_cta": t.systems_per_cta, "units": int(nu.value)}
 
     def close(self):
         if getattr(self, "h", None):

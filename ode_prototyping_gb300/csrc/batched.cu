@@ -7,15 +7,19 @@
 // (RKEmbeddedParallel.hpp:13-81) exactly as the single-system integrator
 // does; only the scheduling differs:
 //   * work units are (system, i-tile) pairs ordered by decreasing cost; a
-//     persistent stage kernel (grid = a multiple of the SM count) takes units
+//     persistent stage kernel (grid = a multiple of the SM count) takes them
 //     round-robin, computes the tile's accelerations against all bodies of
 //     its system and runs the shared stage epilogue;
+//   * with G systems per CTA, systems small enough for one warp group's tile
+//     share a CTA: each of G warp groups (own named barrier, own slice of
+//     the shared buffers) integrates one whole small system;
 //   * one warp per system reduces its tile partials in tile order and applies
 //     that system's controller;
 //   * an attempt (S stage launches + 1 control launch) is captured once in a
 //     CUDA graph and replayed; systems that have reached tf skip their units;
-//   * the tile geometry and grid size are chosen by an autotuner that times
-//     the candidates on the actual batch.
+//   * the tile geometry (threads, lanes, bodies per thread, systems per CTA)
+//     and the grid size are chosen by an autotuner that times the candidates
+//     on the actual batch.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -55,6 +59,9 @@ struct BUnit {
 struct BatchParams {
   const BSys* sys;
   const BUnit* units;
+  const int2* work;      // work items: (first unit, 0) for a whole-CTA unit,
+                         // (first unit, count) for count systems sharing a CTA
+  long long n_work;
   const int* sys_units;  // unit ids of each system in tile order
   const int* body_sys;   // system of each body (packing)
   long long n_units;
@@ -74,90 +81,161 @@ struct BatchParams {
   const void* mlp;       // learned proposer (device copy) or null
 };
 
-template <int PREC, int T, int L, int BPT>
+// Reductions over the TG threads of one group (the whole CTA or a warp
+// group sharing it): the tree of block_sum / block_max.
+template <int TG, class G>
+__device__ __forceinline__ double group_sum(double v, double* red, const G& grp) {
+  const unsigned t = grp.tid();
+  red[t] = v;
+  grp.sync();
+  for (int st = TG / 2; st > 0; st /= 2) {
+    if ((int)t < st) red[t] = dadd(red[t], red[t + st]);
+    grp.sync();
+  }
+  const double r = red[0];
+  grp.sync();
+  return r;
+}
+
+template <int TG, class G>
+__device__ __forceinline__ double group_max(double v, double* red, const G& grp) {
+  const unsigned t = grp.tid();
+  red[t] = v;
+  grp.sync();
+  for (int st = TG / 2; st > 0; st /= 2) {
+    if ((int)t < st) red[t] = fmax(red[t], red[t + st]);
+    grp.sync();
+  }
+  const double r = red[0];
+  grp.sync();
+  return r;
+}
+
+// Shared-memory bytes of the partner staging of TG threads.
+template <int PREC, int TG>
+constexpr int batch_smem_bytes() {
+  return PREC == GB_PREC_F64 ? 32 * TG
+                             : (TG <= 128 ? jp_smem_bytes<TG>() : (int)sizeof(PackedBody) * TG);
+}
+
+// One unit (system, i-tile) of one stage, run by TG threads (the whole CTA,
+// or one warp group of it): the tile's accelerations against every body of
+// its system, then the shared stage epilogue for the tile's bodies.
+template <int PREC, int TG, int L, int BPT, class G>
+__device__ __forceinline__ void stage_unit(const DevTableau& tab, const BatchParams& P, int s,
+                                           long long u, unsigned char* sh_raw,
+                                           double (*part)[3], double* red, const G& grp) {
+  constexpr int BI = (TG / L) * BPT;
+  // TG <= 128: the packed loop over pairs of partners (one or two bodies per thread)
+  constexpr bool PK = PREC == GB_PREC_MIXED && TG <= 128;
+  const int S = tab.n_stages;
+  const BUnit un = P.units[u];
+  const BSys sy = P.sys[un.sys];
+  const Ctrl* C = P.ctrl + un.sys;
+  if (C->done) return;
+  const int cur = C->cur;
+  const double dt = C->dt;
+  const int k0_valid = C->k0_valid;
+  const int k0slot = C->k0slot;
+  const int px = C->px;
+  const long long n = sy.n;
+  const double* x0 = P.ring + (long long)cur * P.total_var + sy.var_off;
+  const double* ysrc = (s == 0) ? x0 : P.Y + (long long)(s & 1) * P.total_var + sy.var_off;
+  const long long i0 = (long long)un.tile * BI;
+  const bool skip_force = (s == 0 && k0_valid);
+  if (!skip_force) {
+    if constexpr (PREC == GB_PREC_F64) {
+      double* sh_pos = reinterpret_cast<double*>(sh_raw);
+      force_f64_cta<TG, L>(ysrc, n, i0, 0, n, sy.eps2, nullptr, sh_pos, sh_pos + 3 * TG, part,
+                           true, grp);
+    } else {
+      const PackedBody* src = (s == 0) ? P.PX + (long long)px * P.total_bodies + sy.body_off
+                                       : P.PY + (long long)(s & 1) * P.total_bodies + sy.body_off;
+      if constexpr (PK) {
+        force_mixed_cta_jp<TG, L, BPT>(src, n, i0, 0, n, sy.eps2f, sh_raw, part, nullptr, 0,
+                                       grp);
+      } else {
+        static_assert(std::is_same_v<G, WholeCta>, "scalar loop: whole CTAs only");
+        force_mixed_cta<TG, L, BPT, true>(src, n, i0, 0, n, sy.eps2f,
+                                          reinterpret_cast<PackedBody*>(sh_raw), part);
+      }
+    }
+  }
+  grp.sync();
+  const bool last = (s == S - 1);
+  EpiCtx E;
+  E.tab = &tab;
+  E.s = s;
+  E.S = S;
+  E.k0slot = k0slot;
+  E.skip_force = skip_force;
+  E.last = last;
+  E.exact = false;
+  E.dt = dt;
+  E.n = n;
+  E.x0 = x0;
+  E.ysrc = ysrc;
+  E.ks = P.ks + sy.var_off;
+  E.kstride = P.total_var;
+  E.ynext = P.Y + (long long)((s + 1) & 1) * P.total_var + sy.var_off;
+  E.xnew = P.ring + (long long)((cur + 1) & 1) * P.total_var + sy.var_off;
+  E.pnext = (last ? P.PX + (long long)(px ^ 1) * P.total_bodies
+                  : P.PY + (long long)((s + 1) & 1) * P.total_bodies) +
+            sy.body_off;
+  E.atol = nullptr;
+  E.rtol = nullptr;
+  E.atol_s = sy.atol;
+  E.rtol_s = sy.rtol;
+  E.masses = nullptr;
+  E.mass = sy.mass;
+  E.cref = P.cref + 3 * un.sys;
+  E.sq = nullptr;
+  const long long nb = min((long long)BI, n - i0);
+  double sq_acc = 0.0, amax = 0.0;
+  for (int b = grp.tid(); b < nb; b += TG) body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
+  if (last) {
+    const double m = group_max<TG>(amax, red, grp);
+    if (grp.tid() == 0) P.aux[u] = m;
+  }
+  if (last) {
+    const double ts = group_sum<TG>(sq_acc, red, grp);
+    if (grp.tid() == 0) P.partials[u] = ts;
+  }
+  grp.sync();
+}
+
+// Persistent stage kernel over work items taken round-robin.  An item is one
+// unit run by the whole CTA, or (G > 1) up to G small systems that share the
+// CTA: warp group g of T / G threads, with its own named barrier and its own
+// slice of the shared buffers, integrates one whole system (its single tile).
+template <int PREC, int T, int L, int BPT, int G>
 __global__ void __launch_bounds__(T)
     batch_stage_kernel(const __grid_constant__ DevTableau tab,
                        const __grid_constant__ BatchParams P, int s) {
+  static_assert(G == 1 || (T / G >= 32 && T <= 128 && (T / G / L) * BPT >= 1),
+                "systems per CTA: warp groups of the packed loop");
   constexpr int BI = (T / L) * BPT;
-  // T <= 128: the packed loop over pairs of partners (one or two bodies per thread)
-  constexpr bool PK = PREC == GB_PREC_MIXED && T <= 128;
-  constexpr int SMEM_BODY_BYTES =
-      PREC == GB_PREC_F64 ? 32 * T : (PK ? jp_smem_bytes<T>() : (int)sizeof(PackedBody) * T);
+  constexpr int SMEM_BODY_BYTES = batch_smem_bytes<PREC, T>();
   __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
   __shared__ double part[BI][3];
   __shared__ double red[T];
-  const int S = tab.n_stages;
-  for (long long u = blockIdx.x; u < P.n_units; u += gridDim.x) {
-    const BUnit un = P.units[u];
-    const BSys sy = P.sys[un.sys];
-    const Ctrl* C = P.ctrl + un.sys;
-    if (C->done) continue;
-    const int cur = C->cur;
-    const double dt = C->dt;
-    const int k0_valid = C->k0_valid;
-    const int k0slot = C->k0slot;
-    const int px = C->px;
-    const long long n = sy.n;
-    const double* x0 = P.ring + (long long)cur * P.total_var + sy.var_off;
-    const double* ysrc = (s == 0) ? x0 : P.Y + (long long)(s & 1) * P.total_var + sy.var_off;
-    const long long i0 = (long long)un.tile * BI;
-    const bool skip_force = (s == 0 && k0_valid);
-    if (!skip_force) {
-      if constexpr (PREC == GB_PREC_F64) {
-        double* sh_pos = reinterpret_cast<double*>(sh_raw);
-        force_f64_cta<T, L>(ysrc, n, i0, 0, n, sy.eps2, nullptr, sh_pos, sh_pos + 3 * T, part,
-                            true);
-      } else {
-        const PackedBody* src = (s == 0) ? P.PX + (long long)px * P.total_bodies + sy.body_off
-                                         : P.PY + (long long)(s & 1) * P.total_bodies + sy.body_off;
-        if constexpr (PK)
-          force_mixed_cta_jp<T, L, BPT>(src, n, i0, 0, n, sy.eps2f, sh_raw, part);
-        else
-          force_mixed_cta<T, L, BPT, true>(src, n, i0, 0, n, sy.eps2f,
-                                           reinterpret_cast<PackedBody*>(sh_raw), part);
+  for (long long w = blockIdx.x; w < P.n_work; w += gridDim.x) {
+    const int2 item = P.work[w];
+    if constexpr (G == 1) {
+      stage_unit<PREC, T, L, BPT>(tab, P, s, item.x, sh_raw, part, red, WholeCta{});
+    } else if (item.y == 0) {
+      stage_unit<PREC, T, L, BPT>(tab, P, s, item.x, sh_raw, part, red, WholeCta{});
+    } else {
+      constexpr int TG = T / G;
+      const int g = (int)threadIdx.x / TG;
+      if (g < item.y) {
+        const WarpGroup<TG> grp{threadIdx.x % TG, 1 + g};
+        stage_unit<PREC, TG, L, BPT>(tab, P, s, item.x + g,
+                                     sh_raw + g * batch_smem_bytes<PREC, TG>(), part + g * (BI / G),
+                                     red + g * TG, grp);
       }
+      __syncthreads();
     }
-    __syncthreads();
-    const bool last = (s == S - 1);
-    EpiCtx E;
-    E.tab = &tab;
-    E.s = s;
-    E.S = S;
-    E.k0slot = k0slot;
-    E.skip_force = skip_force;
-    E.last = last;
-    E.exact = false;
-    E.dt = dt;
-    E.n = n;
-    E.x0 = x0;
-    E.ysrc = ysrc;
-    E.ks = P.ks + sy.var_off;
-    E.kstride = P.total_var;
-    E.ynext = P.Y + (long long)((s + 1) & 1) * P.total_var + sy.var_off;
-    E.xnew = P.ring + (long long)((cur + 1) & 1) * P.total_var + sy.var_off;
-    E.pnext = (last ? P.PX + (long long)(px ^ 1) * P.total_bodies
-                    : P.PY + (long long)((s + 1) & 1) * P.total_bodies) +
-              sy.body_off;
-    E.atol = nullptr;
-    E.rtol = nullptr;
-    E.atol_s = sy.atol;
-    E.rtol_s = sy.rtol;
-    E.masses = nullptr;
-    E.mass = sy.mass;
-    E.cref = P.cref + 3 * un.sys;
-    E.sq = nullptr;
-    const long long nb = min((long long)BI, n - i0);
-    double sq_acc = 0.0, amax = 0.0;
-    for (int b = threadIdx.x; b < nb; b += T) body_epilogue<PREC>(E, i0 + b, part[b], sq_acc, amax);
-    if (last) {
-      const double m = block_max(amax, red);
-      if (threadIdx.x == 0) P.aux[u] = m;
-    }
-    if (last) {
-      const double ts = block_sum(sq_acc, red);
-      if (threadIdx.x == 0) P.partials[u] = ts;
-    }
-    __syncthreads();
   }
 }
 
@@ -213,42 +291,70 @@ __global__ void __launch_bounds__(128)
 }
 
 // ---- start-up (per-system initial step, estimate_initial_step :170-200) ----
-template <int PREC, int T, int L, int BPT>
+// One unit's right-hand side (positions' derivative = velocities, then the
+// accelerations), run by TG threads.
+template <int PREC, int TG, int L, int BPT, class G>
+__device__ __forceinline__ void rhs_unit(const BatchParams& P, long long u,
+                                         const double* __restrict__ x,
+                                         const PackedBody* __restrict__ packed,
+                                         double* __restrict__ out, unsigned char* sh_raw,
+                                         double (*part)[3], const G& grp) {
+  constexpr int BI = (TG / L) * BPT;
+  constexpr bool PK = PREC == GB_PREC_MIXED && TG <= 128;
+  const BUnit un = P.units[u];
+  const BSys sy = P.sys[un.sys];
+  const long long n = sy.n;
+  const long long i0 = (long long)un.tile * BI;
+  const double* xs = x + sy.var_off;
+  if constexpr (PREC == GB_PREC_F64) {
+    double* sh_pos = reinterpret_cast<double*>(sh_raw);
+    force_f64_cta<TG, L>(xs, n, i0, 0, n, sy.eps2, nullptr, sh_pos, sh_pos + 3 * TG, part, false,
+                         grp);
+  } else {
+    if constexpr (PK) {
+      force_mixed_cta_jp<TG, L, BPT>(packed + sy.body_off, n, i0, 0, n, sy.eps2f, sh_raw, part,
+                                     nullptr, 0, grp);
+    } else {
+      static_assert(std::is_same_v<G, WholeCta>, "scalar loop: whole CTAs only");
+      force_mixed_cta<TG, L, BPT, true>(packed + sy.body_off, n, i0, 0, n, sy.eps2f,
+                                        reinterpret_cast<PackedBody*>(sh_raw), part);
+    }
+  }
+  grp.sync();
+  const long long nb = min((long long)BI, n - i0);
+  double* o = out + sy.var_off;
+  for (int e = grp.tid(); e < 3 * nb; e += TG) {
+    const long long g = 3 * i0 + e;
+    o[g] = xs[3 * n + g];
+    o[3 * n + g] = dmul(part[e / 3][e % 3], sy.mass);
+  }
+  grp.sync();
+}
+
+template <int PREC, int T, int L, int BPT, int G>
 __global__ void __launch_bounds__(T)
     batch_rhs_kernel(const __grid_constant__ BatchParams P, const double* __restrict__ x,
                      const PackedBody* __restrict__ packed, double* __restrict__ out) {
   constexpr int BI = (T / L) * BPT;
-  // T <= 128: the packed loop over pairs of partners (one or two bodies per thread)
-  constexpr bool PK = PREC == GB_PREC_MIXED && T <= 128;
-  constexpr int SMEM_BODY_BYTES =
-      PREC == GB_PREC_F64 ? 32 * T : (PK ? jp_smem_bytes<T>() : (int)sizeof(PackedBody) * T);
-  __shared__ __align__(16) unsigned char sh_raw[SMEM_BODY_BYTES];
+  __shared__ __align__(16) unsigned char sh_raw[batch_smem_bytes<PREC, T>()];
   __shared__ double part[BI][3];
-  for (long long u = blockIdx.x; u < P.n_units; u += gridDim.x) {
-    const BUnit un = P.units[u];
-    const BSys sy = P.sys[un.sys];
-    const long long n = sy.n;
-    const long long i0 = (long long)un.tile * BI;
-    const double* xs = x + sy.var_off;
-    if constexpr (PREC == GB_PREC_F64) {
-      double* sh_pos = reinterpret_cast<double*>(sh_raw);
-      force_f64_cta<T, L>(xs, n, i0, 0, n, sy.eps2, nullptr, sh_pos, sh_pos + 3 * T, part);
+  for (long long w = blockIdx.x; w < P.n_work; w += gridDim.x) {
+    const int2 item = P.work[w];
+    if constexpr (G == 1) {
+      rhs_unit<PREC, T, L, BPT>(P, item.x, x, packed, out, sh_raw, part, WholeCta{});
+    } else if (item.y == 0) {
+      rhs_unit<PREC, T, L, BPT>(P, item.x, x, packed, out, sh_raw, part, WholeCta{});
     } else {
-      if constexpr (PK)
-        force_mixed_cta_jp<T, L, BPT>(packed + sy.body_off, n, i0, 0, n, sy.eps2f, sh_raw, part);
-      else
-        force_mixed_cta<T, L, BPT, true>(packed + sy.body_off, n, i0, 0, n, sy.eps2f,
-                                         reinterpret_cast<PackedBody*>(sh_raw), part);
+      constexpr int TG = T / G;
+      const int g = (int)threadIdx.x / TG;
+      if (g < item.y) {
+        const WarpGroup<TG> grp{threadIdx.x % TG, 1 + g};
+        rhs_unit<PREC, TG, L, BPT>(P, item.x + g, x, packed, out,
+                                   sh_raw + g * batch_smem_bytes<PREC, TG>(), part + g * (BI / G),
+                                   grp);
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    const long long nb = min((long long)BI, n - i0);
-    double* o = out + sy.var_off;
-    for (int e = threadIdx.x; e < 3 * nb; e += T) {
-      const long long g = 3 * i0 + e;
-      o[g] = xs[3 * n + g];
-      o[3 * n + g] = dmul(part[e / 3][e % 3], sy.mass);
-    }
-    __syncthreads();
   }
 }
 
@@ -380,21 +486,35 @@ struct BatchKernels {
   const void* rhs;
 };
 
-template <int PREC, int T, int L, int BPT>
+template <int PREC, int T, int L, int BPT, int G>
 BatchKernels kernels_of() {
-  return {(const void*)batch_stage_kernel<PREC, T, L, BPT>,
-          (const void*)batch_rhs_kernel<PREC, T, L, BPT>};
+  return {(const void*)batch_stage_kernel<PREC, T, L, BPT, G>,
+          (const void*)batch_rhs_kernel<PREC, T, L, BPT, G>};
 }
 
-bool pick_batch(int prec, int T, int L, int BPT, BatchKernels* k) {
-#define GB_BK(P_, T_, L_, B_) \
-  if (prec == P_ && T == T_ && L == L_ && BPT == B_) { *k = kernels_of<P_, T_, L_, B_>(); return true; }
-  GB_BK(GB_PREC_MIXED, 128, 1, 1) GB_BK(GB_PREC_MIXED, 128, 2, 1) GB_BK(GB_PREC_MIXED, 128, 4, 1)
-  GB_BK(GB_PREC_MIXED, 128, 1, 2) GB_BK(GB_PREC_MIXED, 128, 2, 2) GB_BK(GB_PREC_MIXED, 128, 4, 2)
-  GB_BK(GB_PREC_MIXED, 256, 2, 1) GB_BK(GB_PREC_MIXED, 256, 4, 1) GB_BK(GB_PREC_MIXED, 256, 2, 2)
-  GB_BK(GB_PREC_MIXED, 256, 4, 2) GB_BK(GB_PREC_MIXED, 64, 1, 1) GB_BK(GB_PREC_MIXED, 64, 2, 1)
-  GB_BK(GB_PREC_F64, 128, 1, 1) GB_BK(GB_PREC_F64, 128, 2, 1) GB_BK(GB_PREC_F64, 128, 4, 1)
-  GB_BK(GB_PREC_F64, 64, 1, 1) GB_BK(GB_PREC_F64, 64, 2, 1)
+// Geometries built into the library: (precision, threads, lanes, bodies per
+// thread, systems per CTA).
+bool pick_batch(int prec, int T, int L, int BPT, int G, BatchKernels* k) {
+#define GB_BK(P_, T_, L_, B_, G_)                                            \
+  if (prec == P_ && T == T_ && L == L_ && BPT == B_ && G == G_) {            \
+    *k = kernels_of<P_, T_, L_, B_, G_>();                                   \
+    return true;                                                             \
+  }
+  GB_BK(GB_PREC_MIXED, 128, 1, 1, 1) GB_BK(GB_PREC_MIXED, 128, 2, 1, 1)
+  GB_BK(GB_PREC_MIXED, 128, 4, 1, 1) GB_BK(GB_PREC_MIXED, 128, 1, 2, 1)
+  GB_BK(GB_PREC_MIXED, 128, 2, 2, 1) GB_BK(GB_PREC_MIXED, 128, 4, 2, 1)
+  GB_BK(GB_PREC_MIXED, 256, 2, 1, 1) GB_BK(GB_PREC_MIXED, 256, 4, 1, 1)
+  GB_BK(GB_PREC_MIXED, 256, 2, 2, 1) GB_BK(GB_PREC_MIXED, 256, 4, 2, 1)
+  GB_BK(GB_PREC_MIXED, 64, 1, 1, 1) GB_BK(GB_PREC_MIXED, 64, 2, 1, 1)
+  GB_BK(GB_PREC_MIXED, 128, 1, 1, 2) GB_BK(GB_PREC_MIXED, 128, 1, 1, 4)
+  GB_BK(GB_PREC_MIXED, 128, 2, 1, 2) GB_BK(GB_PREC_MIXED, 128, 1, 2, 2)
+  GB_BK(GB_PREC_MIXED, 128, 1, 2, 4) GB_BK(GB_PREC_MIXED, 128, 2, 2, 2)
+  GB_BK(GB_PREC_MIXED, 64, 1, 1, 2)
+  GB_BK(GB_PREC_F64, 128, 1, 1, 1) GB_BK(GB_PREC_F64, 128, 2, 1, 1)
+  GB_BK(GB_PREC_F64, 128, 4, 1, 1) GB_BK(GB_PREC_F64, 64, 1, 1, 1)
+  GB_BK(GB_PREC_F64, 64, 2, 1, 1)
+  GB_BK(GB_PREC_F64, 128, 1, 1, 2) GB_BK(GB_PREC_F64, 128, 1, 1, 4)
+  GB_BK(GB_PREC_F64, 128, 2, 1, 2) GB_BK(GB_PREC_F64, 64, 1, 1, 2)
 #undef GB_BK
   return false;
 }
@@ -414,14 +534,15 @@ struct gb_batch_s {
   std::vector<long long> n;
   std::vector<double> soft, mass;
   // geometry
-  int T = 128, L = 2, BPT = 1, grid = 0;
+  int T = 128, L = 2, BPT = 1, G = 1, grid = 0;
   gb::BatchKernels k{};
   // device
   gb::BSys* sys = nullptr;
   gb::BUnit* units = nullptr;
+  int2* work = nullptr;
   int* sys_units = nullptr;
   int* body_sys = nullptr;
-  long long n_units = 0, max_units = 0;
+  long long n_units = 0, n_work = 0, max_units = 0;
   gb::Ctrl* ctrl = nullptr;
   double *ring = nullptr, *ks = nullptr, *Y = nullptr, *cref = nullptr, *partials = nullptr,
          *aux = nullptr, *dscal = nullptr, *tv = nullptr;
@@ -457,10 +578,16 @@ int wait_ev(cudaEvent_t ev, double timeout_s) {
   }
 }
 
-// (Re)builds the unit list for the current tile size: units ordered by
-// decreasing cost (tile bodies x system bodies), then round-robin on the grid.
+// (Re)builds the unit list for the current geometry: units (system, i-tile)
+// ordered by decreasing cost (tile bodies x system bodies).  With G systems
+// per CTA, every system that fits one warp group's tile (n <= BI / G) is one
+// unit, and such units are grouped G at a time, in cost order, into work
+// items that share a CTA; every other unit is a work item of its own.  Work
+// items are taken round-robin by the persistent grid.
 int build_units(gb_batch_s* b) {
   const int BI = (b->T / b->L) * b->BPT;
+  const int G = b->G;
+  const long long small_n = G > 1 ? BI / G : 0;
   std::vector<BUnit> units;
   std::vector<long long> cost;
   for (int k = 0; k < b->n_sys; ++k) {
@@ -474,8 +601,26 @@ int build_units(gb_batch_s* b) {
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](size_t x, size_t y) { return cost[x] > cost[y]; });
-  std::vector<BUnit> sorted(units.size());
-  for (size_t i = 0; i < order.size(); ++i) sorted[i] = units[order[i]];
+  std::vector<BUnit> sorted;
+  std::vector<int2> work;
+  std::vector<size_t> pending;
+  sorted.reserve(units.size());
+  auto flush_group = [&]() {
+    if (pending.empty()) return;
+    work.push_back(make_int2((int)sorted.size(), (int)pending.size()));
+    for (size_t i : pending) sorted.push_back(units[i]);
+    pending.clear();
+  };
+  for (size_t i : order) {
+    if (G > 1 && b->n[units[i].sys] <= small_n) {
+      pending.push_back(i);
+      if ((int)pending.size() == G) flush_group();
+    } else {
+      work.push_back(make_int2((int)sorted.size(), 0));
+      sorted.push_back(units[i]);
+    }
+  }
+  flush_group();
   // unit ids of each system in tile order
   std::vector<BSys> hs(b->n_sys);
   std::vector<int> su(sorted.size());
@@ -513,18 +658,23 @@ int build_units(gb_batch_s* b) {
   GB_CUDA_TRY(cudaMemcpy(b->sys, hs.data(), hs.size() * sizeof(BSys), cudaMemcpyHostToDevice));
   GB_CUDA_TRY(cudaMemcpy(b->units, sorted.data(), sorted.size() * sizeof(BUnit),
                          cudaMemcpyHostToDevice));
+  GB_CUDA_TRY(cudaMemcpy(b->work, work.data(), work.size() * sizeof(int2),
+                         cudaMemcpyHostToDevice));
+  b->n_work = (long long)work.size();
+  b->P.n_work = b->n_work;
   GB_CUDA_TRY(cudaMemcpy(b->sys_units, su.data(), su.size() * sizeof(int),
                          cudaMemcpyHostToDevice));
   b->P.n_units = b->n_units;
   return GB_OK;
 }
 
-int set_geometry(gb_batch_s* b, int T, int L, int BPT, int grid) {
+int set_geometry(gb_batch_s* b, int T, int L, int BPT, int G, int grid) {
   BatchKernels k;
-  if (!pick_batch(b->opts.precision, T, L, BPT, &k)) return GB_ERR_UNSUPPORTED;
+  if (!pick_batch(b->opts.precision, T, L, BPT, G, &k)) return GB_ERR_UNSUPPORTED;
   b->T = T;
   b->L = L;
   b->BPT = BPT;
+  b->G = G;
   b->k = k;
   b->grid = grid > 0 ? grid : num_sms() * 8;
   return build_units(b);
@@ -581,9 +731,9 @@ int read_ctrl(gb_batch_s* b) {
 void free_batch(gb_batch_s* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  void* bufs[] = {b->sys,  b->units, b->sys_units, b->body_sys, b->ctrl, b->ring, b->ks,
-                  b->Y,    b->cref,  b->partials,  b->aux,      b->dscal, b->tv,  b->PX,
-                  b->PY,   b->n_done, b->mlp_dev};
+  void* bufs[] = {b->sys,  b->units, b->work,     b->sys_units, b->body_sys, b->ctrl,
+                  b->ring, b->ks,    b->Y,        b->cref,      b->partials, b->aux,
+                  b->dscal, b->tv,   b->PX,       b->PY,        b->n_done,   b->mlp_dev};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (b->hctrl) cudaFreeHost(b->hctrl);
@@ -650,6 +800,7 @@ extern "C" int gb_batch_create(const gb_tableau* tab, int32_t n_sys, const int64
   };
   alloc((void**)&b->sys, n_sys * sizeof(BSys));
   alloc((void**)&b->units, b->max_units * sizeof(BUnit));
+  alloc((void**)&b->work, b->max_units * sizeof(int2));
   alloc((void**)&b->sys_units, b->max_units * sizeof(int));
   alloc((void**)&b->body_sys, tb * sizeof(int));
   alloc((void**)&b->ctrl, n_sys * sizeof(Ctrl));
@@ -688,6 +839,7 @@ extern "C" int gb_batch_create(const gb_tableau* tab, int32_t n_sys, const int64
   BatchParams& P = b->P;
   P.sys = b->sys;
   P.units = b->units;
+  P.work = b->work;
   P.sys_units = b->sys_units;
   P.body_sys = b->body_sys;
   P.n_sys = n_sys;
@@ -714,7 +866,8 @@ extern "C" int gb_batch_create(const gb_tableau* tab, int32_t n_sys, const int64
   const int BPT = opts.precision == GB_PREC_F64
                       ? 1
                       : (opts.tiling.bodies_per_thread > 0 ? opts.tiling.bodies_per_thread : 1);
-  int rc = set_geometry(b, T, L, BPT, opts.tiling.grid_ctas);
+  const int G = opts.tiling.systems_per_cta > 0 ? opts.tiling.systems_per_cta : 1;
+  int rc = set_geometry(b, T, L, BPT, G, opts.tiling.grid_ctas);
   if (rc != GB_OK) return fail(rc);
   *out = b;
   return GB_OK;
@@ -863,34 +1016,43 @@ extern "C" int gb_batch_launch_stage(gb_batch b, int32_t stage) {
 
 // Times every candidate geometry on the batch (stage 1, `reps` launches each)
 // and keeps the fastest; rebuilds the unit list and the graph.  Must follow
-// gb_batch_start (the stage buffers must hold a valid attempt).
+// gb_batch_start (the stage buffers must hold a valid attempt).  Candidates
+// with several systems per CTA are timed only where some system fits a warp
+// group's tile (otherwise they are the one-system geometry again).
 extern "C" int gb_batch_autotune(gb_batch b, int32_t reps, gb_batch_tiling* chosen,
                                  double* best_ms) {
   if (!b || !b->started || b->S < 3) return GB_ERR_INVALID_ARGUMENT;
   if (reps < 1) reps = 3;
   struct Cand {
-    int T, L, BPT, gridmul;
+    int T, L, BPT, G, gridmul;
   };
   std::vector<Cand> cands;
   const int sms = num_sms();
+  const long long n_min = *std::min_element(b->n.begin(), b->n.end());
+  auto add = [&](int T, int L, int BPT, int G) {
+    if (G > 1 && n_min > (long long)((T / L) * BPT / G)) return;
+    for (int gm : {4, 8, 16}) cands.push_back({T, L, BPT, G, gm});
+  };
   if (b->opts.precision == GB_PREC_MIXED) {
-    const int tl[][3] = {{128, 1, 1}, {128, 2, 1}, {128, 4, 1}, {128, 1, 2}, {128, 2, 2},
-                         {128, 4, 2}, {256, 2, 1}, {256, 4, 1}, {256, 2, 2}, {256, 4, 2},
-                         {64, 1, 1},  {64, 2, 1}};
-    for (auto& t : tl)
-      for (int gm : {4, 8, 16}) cands.push_back({t[0], t[1], t[2], gm});
+    const int tl[][4] = {{128, 1, 1, 1}, {128, 2, 1, 1}, {128, 4, 1, 1}, {128, 1, 2, 1},
+                         {128, 2, 2, 1}, {128, 4, 2, 1}, {256, 2, 1, 1}, {256, 4, 1, 1},
+                         {256, 2, 2, 1}, {256, 4, 2, 1}, {64, 1, 1, 1},  {64, 2, 1, 1},
+                         {128, 1, 1, 2}, {128, 1, 1, 4}, {128, 2, 1, 2}, {128, 1, 2, 2},
+                         {128, 1, 2, 4}, {128, 2, 2, 2}, {64, 1, 1, 2}};
+    for (auto& t : tl) add(t[0], t[1], t[2], t[3]);
   } else {
-    const int tl[][3] = {{128, 1, 1}, {128, 2, 1}, {128, 4, 1}, {64, 1, 1}, {64, 2, 1}};
-    for (auto& t : tl)
-      for (int gm : {4, 8, 16}) cands.push_back({t[0], t[1], t[2], gm});
+    const int tl[][4] = {{128, 1, 1, 1}, {128, 2, 1, 1}, {128, 4, 1, 1}, {64, 1, 1, 1},
+                         {64, 2, 1, 1},  {128, 1, 1, 2}, {128, 1, 1, 4}, {128, 2, 1, 2},
+                         {64, 1, 1, 2}};
+    for (auto& t : tl) add(t[0], t[1], t[2], t[3]);
   }
   cudaEvent_t e0, e1;
   GB_CUDA_TRY(cudaEventCreate(&e0));
   GB_CUDA_TRY(cudaEventCreate(&e1));
   double best = 1e300;
-  Cand bc = {b->T, b->L, b->BPT, b->grid / sms};
+  Cand bc = {b->T, b->L, b->BPT, b->G, b->grid / sms};
   for (const Cand& c : cands) {
-    if (set_geometry(b, c.T, c.L, c.BPT, c.gridmul * sms) != GB_OK) continue;
+    if (set_geometry(b, c.T, c.L, c.BPT, c.G, c.gridmul * sms) != GB_OK) continue;
     GB_TRY(launch_stage(b, 1));  // warm
     GB_CUDA_TRY(cudaEventRecord(e0, b->stream));
     for (int r = 0; r < reps; ++r) GB_TRY(launch_stage(b, 1 + r % (b->S - 2)));
@@ -905,13 +1067,14 @@ extern "C" int gb_batch_autotune(gb_batch b, int32_t reps, gb_batch_tiling* chos
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  GB_TRY(set_geometry(b, bc.T, bc.L, bc.BPT, bc.gridmul * sms));
+  GB_TRY(set_geometry(b, bc.T, bc.L, bc.BPT, bc.G, bc.gridmul * sms));
   GB_TRY(rebuild_graph(b));
   if (chosen) {
     chosen->threads_per_cta = bc.T;
     chosen->lanes = bc.L;
     chosen->bodies_per_thread = bc.BPT;
     chosen->grid_ctas = bc.gridmul * sms;
+    chosen->systems_per_cta = bc.G;
   }
   if (best_ms) *best_ms = best;
   return GB_OK;
@@ -923,6 +1086,7 @@ extern "C" int gb_batch_geometry(gb_batch b, gb_batch_tiling* t, int64_t* n_unit
   t->lanes = b->L;
   t->bodies_per_thread = b->BPT;
   t->grid_ctas = b->grid;
+  t->systems_per_cta = b->G;
   if (n_units) *n_units = b->n_units;
   return GB_OK;
 }

@@ -15,6 +15,8 @@
 //     -(d/den) == (-d)/den), so the FP64 sums match it bit for bit.
 #pragma once
 
+#include <type_traits>
+
 #include "gb_internal.cuh"
 
 namespace gb {
@@ -116,22 +118,53 @@ __device__ __forceinline__ void cluster_combine_rows(double (*part)[3], int rank
 }
 
 // ---------------------------------------------------------------------------
-// FP64: partial sums of one CTA over its partner chunk.  sh_pos holds 3*T
-// doubles, sh_m T doubles (per-body masses only).  Results land in part[b].
-// fast = false: every pair term in the reference's operation order (IEEE
-// sqrt and divisions, NBodyODE.hpp:89-98), summed with IEEE adds; fast =
-// true: r^-3 from the refined reciprocal square root (rinv3_f64) and fused
-// multiply-add accumulation, a few ulp per term from the reference's.
+// The threads that run one force tile together: the whole CTA (barrier 0,
+// __syncthreads), or one of several groups of T consecutive threads (whole
+// warps) that share a CTA, each synchronised by its own named barrier -- the
+// batched integrator runs one small system per group.
 // ---------------------------------------------------------------------------
-template <int T, int L>
+struct WholeCta {
+  __device__ __forceinline__ unsigned tid() const { return threadIdx.x; }
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+
+template <int T>
+struct WarpGroup {
+  static_assert(T % 32 == 0, "a named barrier counts whole warps");
+  unsigned t;  // thread index within the group
+  int bar;     // named barrier id, 1..4 (0 is __syncthreads)
+  __device__ __forceinline__ unsigned tid() const { return t; }
+  __device__ __forceinline__ void sync() const {
+    // immediate ids, so the kernel reserves barriers 0..4 only
+    switch (bar) {
+      case 1: asm volatile("bar.sync 1, %0;" ::"n"(T) : "memory"); break;
+      case 2: asm volatile("bar.sync 2, %0;" ::"n"(T) : "memory"); break;
+      case 3: asm volatile("bar.sync 3, %0;" ::"n"(T) : "memory"); break;
+      default: asm volatile("bar.sync 4, %0;" ::"n"(T) : "memory"); break;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// FP64: partial sums of one CTA (or thread group) over its partner chunk.
+// sh_pos holds 3*T doubles, sh_m T doubles (per-body masses only).  Results
+// land in part[b].  fast = false: every pair term in the reference's
+// operation order (IEEE sqrt and divisions, NBodyODE.hpp:89-98), summed with
+// IEEE adds; fast = true: r^-3 from the refined reciprocal square root
+// (rinv3_f64) and fused multiply-add accumulation, a few ulp per term from
+// the reference's.  With L lanes, lane l takes the partners j = l (mod L) in
+// ascending order whatever T is, so the sums do not depend on the group size.
+// ---------------------------------------------------------------------------
+template <int T, int L, class G = WholeCta>
 __device__ __forceinline__ void force_f64_cta(const double* __restrict__ pos, long long n,
                                               long long i0, long long jb, long long je,
                                               double eps2, const double* __restrict__ masses,
                                               double* sh_pos, double* sh_m, double (*part)[3],
-                                              bool fast = false) {
+                                              bool fast = false, const G& grp = G{}) {
   constexpr int BI = T / L;
-  const int b = threadIdx.x / L;
-  const int l = threadIdx.x % L;
+  const unsigned tid = grp.tid();
+  const int b = tid / L;
+  const int l = tid % L;
   const long long i = i0 + b;
   double xi = 0.0, yi = 0.0, zi = 0.0;
   if (i < n) {
@@ -142,11 +175,11 @@ __device__ __forceinline__ void force_f64_cta(const double* __restrict__ pos, lo
   double sx = 0.0, sy = 0.0, sz = 0.0;
   for (long long j0 = jb; j0 < je; j0 += T) {
     const int cnt = (int)min((long long)T, je - j0);
-    __syncthreads();
-    for (int k = threadIdx.x; k < 3 * cnt; k += T) sh_pos[k] = pos[3 * j0 + k];
+    grp.sync();
+    for (int k = tid; k < 3 * cnt; k += T) sh_pos[k] = pos[3 * j0 + k];
     if (masses)
-      for (int k = threadIdx.x; k < cnt; k += T) sh_m[k] = masses[j0 + k];
-    __syncthreads();
+      for (int k = tid; k < cnt; k += T) sh_m[k] = masses[j0 + k];
+    grp.sync();
     if (i >= n) continue;
     if (fast) {
       for (int jj = l; jj < cnt; jj += L) {
@@ -500,14 +533,16 @@ __device__ __forceinline__ float4 warp_box(float hx, float hy, float hz, bool va
 // runs the pair loop without the close-pair test.  Its terms are the ones the
 // test would have kept, so the sums are bit for bit those of the loop with
 // the test.
-template <int T, int L, int NB = 1, bool PAIRS = false, bool CULL = false>
+template <int T, int L, int NB = 1, bool PAIRS = false, bool CULL = false, class G = WholeCta>
 __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict__ packed,
                                                    long long n, long long i0, long long jb,
                                                    long long je, float eps2, unsigned char* smem,
                                                    double (*part)[3],
                                                    const float4* __restrict__ boxes = nullptr,
-                                                   int cull = 0) {
+                                                   int cull = 0, const G& grp = G{}) {
   static_assert(!CULL || (L == 1 && NB == 1 && T == 128), "culling: 128 one-body threads");
+  static_assert(!CULL || std::is_same_v<G, WholeCta>, "culling: the whole CTA");
+  const unsigned tid = grp.tid();
   constexpr int BG = T / L;  // body groups per CTA (NB bodies each)
   constexpr int JT = 2 * T;  // partners per tile
   // per warp: its box (centre, radius) and the near-pair bound of its bodies,
@@ -515,8 +550,8 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
   __shared__ float sh_wbox[T / 32][5];
   PartnerPair* recs = reinterpret_cast<PartnerPair*>(smem);  // two buffers of T records
   PackedBody* raw = reinterpret_cast<PackedBody*>(smem + 2 * sizeof(PartnerPair) * T);
-  const int g = threadIdx.x / L;
-  const int l = threadIdx.x % L;
+  const int g = tid / L;
+  const int l = tid % L;
   f2_t HX[NB], HY[NB], HZ[NB], LX[NB], LY[NB], LZ[NB];
   int near2[NB];
 #pragma unroll
@@ -564,10 +599,10 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
   // built at the end of tile k into the buffer tile k - 1 used, and one
   // barrier per tile both publishes them and retires tile k's.
   auto issue = [&](long long j0) {
-    PackedBody* dst = raw + 2 * threadIdx.x;
+    PackedBody* dst = raw + 2 * tid;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const long long j = j0 + 2 * threadIdx.x + h;
+      const long long j = j0 + 2 * tid + h;
       if (j < je) {
         cp_async16(&dst[h].hw, &packed[j].hw);
         cp_async16(&dst[h].lo, &packed[j].lo);
@@ -591,11 +626,11 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
       }
       fm = __ballot_sync(0xffffffffu, far);
     }
-    if ((int)threadIdx.x < (cnt + 1) / 2) {
-      const PackedBody a = raw[2 * threadIdx.x];
+    if ((int)tid < (cnt + 1) / 2) {
+      const PackedBody a = raw[2 * tid];
       PackedBody b;
-      if (2 * (int)threadIdx.x + 1 < cnt) {
-        b = raw[2 * threadIdx.x + 1];
+      if (2 * (int)tid + 1 < cnt) {
+        b = raw[2 * tid + 1];
       } else {
         b.hw = make_float4(1e18f, 1e18f, 1e18f, 0.f);
         b.lo = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -604,7 +639,7 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
       r.xy = make_ulonglong2(f2_pack(a.hw.x, b.hw.x), f2_pack(a.hw.y, b.hw.y));
       r.zl = make_ulonglong2(f2_pack(a.hw.z, b.hw.z), f2_pack(a.lo.x, b.lo.x));
       r.yz = make_ulonglong2(f2_pack(a.lo.y, b.lo.y), f2_pack(a.lo.z, b.lo.z));
-      out[threadIdx.x] = r;
+      out[tid] = r;
     }
     return fm;
   };
@@ -615,7 +650,7 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
     fm = build(jb, recs);
     if (jb + JT < je) issue(jb + JT);
   }
-  __syncthreads();
+  grp.sync();
   int buf = 0;
   for (long long j0 = jb; j0 < je; j0 += JT, buf ^= 1) {
     const int cnt = (int)min((long long)JT, je - j0);
@@ -730,7 +765,7 @@ __device__ __forceinline__ void force_mixed_cta_jp(const PackedBody* __restrict_
       fm_next = build(j0 + JT, recs + (buf ^ 1) * T);
       if (j0 + 2 * JT < je) issue(j0 + 2 * JT);
     }
-    __syncthreads();
+    grp.sync();
     fm = fm_next;
   }
   if constexpr (PAIRS) {

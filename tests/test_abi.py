@@ -149,3 +149,37 @@ def test_executor_options_reach_the_c_struct(gb):
     d = gb.Gb300Executor().opts(record=False)
     assert (d.precision, d.controller, d.fsal, d.exact, d.record, d.mlp) == (0, 0, 1, 0, 0, None)
     assert gb.tiling(scalar=True).mixed_variant == 1
+
+
+# ctypes mirror -> C typedef in include/gbode.h
+_STRUCTS = {"GbTableau": "gb_tableau", "GbForceTiling": "gb_force_tiling",
+            "GbMlp": "gb_mlp", "GbStepLog": "gb_step_log", "GbNBodySystem": "gb_nbody_system",
+            "GbIntegrateOpts": "gb_integrate_opts", "GbIntegrateStats": "gb_integrate_stats",
+            "GbBatchTiling": "gb_batch_tiling", "GbBatchOpts": "gb_batch_opts"}
+
+
+def test_struct_layouts_match_the_c_compiler(gb, tmp_path):
+    """Every ctypes mirror has the size and field offsets the C compiler
+    gives the header's struct (a field added on one side only fails here)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gbode.h"', "int main(void) {"]
+    for py, c in _STRUCTS.items():
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({c}));')
+        for f, _ in getattr(gb, py)._fields_:
+            lines.append(f'  printf("{py} {f} %zu\\n", offsetof({c}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", f"-I{os.path.join(ROOT, 'include')}", str(src), "-o",
+                    str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    for line in out.splitlines():
+        py, field, value = line.split()
+        cls = getattr(gb, py)
+        got = C.sizeof(cls) if field == "size" else getattr(cls, field).offset
+        assert got == int(value), (py, field, got, int(value))

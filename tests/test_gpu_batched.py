@@ -140,3 +140,64 @@ def test_batch_pi_controller_matches_single_system(gb, torch_cuda):
         assert np.max(np.abs(b.system_state(x, k) - xk.cpu().numpy())) <= 10 * tol
         it.close()
     b.close()
+
+
+@pytest.mark.parametrize("spc", [2, 4])
+def test_batch_systems_sharing_a_cta_follow_the_oracle(gb, orc, torch_cuda, spc):
+    """Several small systems per CTA (one warp group each): in FP64 every
+    system follows the reference loop (oracle), and the whole batch is bit
+    for bit the batch with one system per CTA (a lane's partner order does
+    not depend on the group size)."""
+    sizes = [33, 64, 100, 129, 7, 250, 1, 20, 50, 31, 64, 12]
+    soft, tol, tf = 0.05, 1e-9, 0.1
+    xs, x0 = _systems(gb, sizes, 140)
+    runs = []
+    for g in (1, spc):
+        b = gb.Batch("DOPRI5", sizes, soft, precision="f64",
+                     tiling=gb.GbBatchTiling(128, 1, 1, 0, g))
+        geo = b.geometry()
+        assert geo["systems_per_cta"] == g
+        b.start(x0, 0.0, tf, tol, tol)
+        assert b.advance() == 0
+        x, t = b.state()
+        runs.append((x.cpu().numpy(), t, b.stats(per_system=True)))
+        b.close()
+    (x1, t1, _), (xg, tg, st) = runs
+    np.testing.assert_array_equal(xg, x1)
+    np.testing.assert_array_equal(tg, t1)
+    for k, n in enumerate(sizes):
+        ode, _ = orc.nbody_ode(n, soft, 1.0 / n)
+        r = orc.integrate("DOPRI5", ode, xs[k], 0.0, tf, tol, tol)
+        assert st["systems"][k]["n_accepted"] == len(r.times) - 1, k
+        assert np.max(np.abs(x1[6 * sum(sizes[:k]):6 * sum(sizes[:k + 1])] - r.states[-1])) \
+            <= 10 * tol, k
+
+
+def test_batch_mixed_systems_sharing_a_cta(gb, torch_cuda):
+    """Mixed precision, two systems of up to 64 bodies per 128-thread CTA:
+    each such system runs the 64-thread packed pair loop, so it is bit for
+    bit the system of a 64-thread batch; every system tracks the FP64 batch
+    to 1e-6."""
+    sizes = [64, 40, 200, 17, 64, 130, 1, 50, 33]
+    soft, tol, tf = 0.05, 1e-9, 0.05
+    xs, x0 = _systems(gb, sizes, 160)
+    ref = gb.Batch("DOPRI5", sizes, soft, precision="f64")
+    ref.start(x0, 0.0, tf, tol, tol)
+    assert ref.advance() == 0
+    xr, _ = ref.state()
+    ref.close()
+    out = {}
+    for key, til in (("grouped", gb.GbBatchTiling(128, 1, 1, 0, 2)),
+                     ("t64", gb.GbBatchTiling(64, 1, 1, 0, 1))):
+        b = gb.Batch("DOPRI5", sizes, soft, precision="mixed", tiling=til)
+        b.start(x0, 0.0, tf, tol, tol)
+        assert b.advance() == 0
+        x, t = b.state()
+        np.testing.assert_allclose(t, tf)
+        assert (x - xr).abs().max().item() <= 1e-6, key
+        out[key] = x.cpu().numpy()
+        b.close()
+    for k, n in enumerate(sizes):
+        if n <= 64:
+            sl = slice(6 * sum(sizes[:k]), 6 * sum(sizes[:k + 1]))
+            np.testing.assert_array_equal(out["grouped"][sl], out["t64"][sl])
