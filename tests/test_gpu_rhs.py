@@ -20,6 +20,22 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
+def _force_scale(x, n, soft, rows=512):
+    """Per body, the sum of the magnitudes of its pair terms, m sum_j
+    |x_j - x_i| / (r^2 + eps^2)^(3/2) (FP64, torch on the GPU): the scale a
+    per-body acceleration error is measured against when the pair terms
+    nearly cancel (a body near the centre of mass has |a_i| << that sum)."""
+    import torch
+    p = torch.as_tensor(np.asarray(x[: 3 * n]).reshape(-1, 3), dtype=torch.float64,
+                        device="cuda")
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    for i0 in range(0, n, rows):
+        d = p[None, :, :] - p[i0:i0 + rows, None, :]
+        r = d.norm(dim=2)
+        out[i0:i0 + rows] = (r / (r * r + soft * soft) ** 1.5).sum(dim=1)
+    return out.cpu().numpy() / n
+
+
 @pytest.mark.parametrize("n,soft", [(2, 0.1), (5, 0.0), (64, 0.05), (1000, 0.01), (1024, 0.01),
                                     (1031, 0.2)])
 def test_rhs_f64_serial_tiling_is_bitwise_reference(gb, orc, torch_cuda, n, soft):
@@ -136,9 +152,17 @@ def test_rhs_mixed_within_1e6_of_fp64(gb, torch_cuda, n, soft, gen, variant):
     a_g, a_r = got[3 * n:].reshape(-1, 3), ref[3 * n:].reshape(-1, 3)
     # normwise relative error of the acceleration field
     assert _rel(a_g, a_r) <= 1e-6, _rel(a_g, a_r)
-    per = np.linalg.norm(a_g - a_r, axis=1) / np.linalg.norm(a_r, axis=1)
-    # per-body: the median body is far inside the bound
+    err = np.linalg.norm(a_g - a_r, axis=1)
+    per = err / np.linalg.norm(a_r, axis=1)
+    # per-body: the median body is far inside the bound, and 99.9 % of the
+    # bodies are within it where there are enough bodies for that quantile
     assert np.median(per) <= 1e-6, np.median(per)
+    if n >= 1024:
+        assert np.quantile(per, 0.999) <= 1e-6, np.quantile(per, 0.999)
+    # every body, against the sum of its pair terms' magnitudes (the error
+    # bound of the pair differences is relative to each term)
+    cond = err / _force_scale(x, n, soft)
+    assert cond.max() <= 1e-6, cond.max()
 
 
 def test_rhs_mixed_masses_and_shift_invariance(gb, torch_cuda):
