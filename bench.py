@@ -74,7 +74,7 @@ FLOPS_PER_INTERACTION = 20  # Nyland, Harris & Prins (GPU Gems 3, ch. 31) conven
 HILO_FP32_OPS = 11.5
 # DRAM bytes (read + write) of one headline stage launch from an ncu capture
 # of the same kernel and geometry (python bench.py --workload stage).
-STAGE_DRAM_BYTES_16384 = 2722816
+STAGE_DRAM_BYTES_16384 = 2652160
 FP64_TFLOPS_NOMINAL = 1.25  # GB300 FP64 (non-tensor), one FMA = 2 FLOP
 
 
@@ -428,13 +428,16 @@ def main():
     ap.add_argument("--learned-config", default="plummer4096_rkf78",
                     help="c4: proposer training/evaluation configuration")
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c2_f64", "c2_tol", "c2_sweep", "c1", "c3", "c4", "c5a", "c5b",
+                    choices=["c2", "c2_f64", "c2_tol", "c2_sweep", "c1", "c3", "c4", "c5a", "c5b", "pipes",
                              "rk_hbm", "stage"],
                     help="c2 (default, the headline), or another configuration")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "pipes":
+        run_pipe_probe()
         return
     if args.workload != "c2":
         run_other_workload(args)
@@ -627,6 +630,20 @@ def _batch_ics(gb, torch, sizes, seeds, kind, eps):
             x = gb.ic_binary_plummer(int(n), int(seed), 0.1, 1e-3, 1e-2)
         xs.append(x)
     return np.concatenate(xs)
+
+
+def run_pipe_probe():
+    """Throughput ceilings for the force kernel's roofline: builds and runs
+    ode_prototyping_gb300/csrc/probe/pipes.cu (scalar and f32x2 FMA, SFU
+    rsqrt, the pair loop alone) and prints its JSON line."""
+    src = os.path.join(ROOT, "ode_prototyping_gb300", "csrc", "probe", "pipes.cu")
+    exe = os.path.join(ROOT, "ode_prototyping_gb300", "_build", "probe_pipes")
+    os.makedirs(os.path.dirname(exe), exist_ok=True)
+    nvcc = "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc"
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", src,
+                    "-o", exe], check=True)
+    r = subprocess.run([exe], check=True, capture_output=True, text=True)
+    print(json.dumps({"workload": "pipes", **json.loads(r.stdout)}), flush=True)
 
 
 def run_other_workload(args):

@@ -306,7 +306,7 @@ __device__ __forceinline__ void split_pre_rows(const DevTableau& tab, const Fuse
 // their pair loops between 45 and 128 us at N = 16384) while an 8-CTA cluster
 // waited for its slowest rank; independent CTAs let the block scheduler
 // refill every SM until the last chunks.  Each CTA runs the pair loop, in
-// which every 64-partner quarter tile whose box is far from the box of a
+// which every 64-partner quarter tile whose box is far from each of a
 // warp's 32 bodies skips the close-pair test for that warp (sorted bodies are
 // compact, so many are), and stores its chunk's sums as FP32 Kahan pairs;
 // the CTAs of a middle band of chunks then finish a slice of the tile's rows
