@@ -423,6 +423,8 @@ def main():
     ap.add_argument("--stage-precision", default="mixed", choices=["mixed", "f64"],
                     help="stage: precision of the integrator")
     ap.add_argument("--tol", type=float, default=1e-9, help="c2_tol: atol = rtol")
+    ap.add_argument("--sweep-tols", default="3e-12,1e-11,3e-11",
+                    help="c2_sweep: tolerances of each controller's sweep (comma-separated)")
     ap.add_argument("--tol-override", type=float, default=None,
                     help="c3 / c5b: atol = rtol instead of the configuration's")
     ap.add_argument("--learned-config", default="plummer4096_rkf78",
@@ -719,14 +721,14 @@ def run_other_workload(args):
         # integrated t = 0 -> 2 (mixed precision) by the reference, PI and
         # learned controllers, each at the tolerances 3e-12, 1e-11, 3e-11; for
         # each controller the time to tf at a common relative energy error
-        # (the geometric mean of the three controllers' errors at 1e-11) is
-        # read off its own sweep by log-log interpolation in the tolerance.
+        # (the geometric mean of the three controllers' errors at the middle
+        # tolerance) is read off its own sweep by log-log interpolation.
         W = WORKLOAD
         n, eps = W["n_particles"], W["softening"]
         x0 = gb.to_device(gb.ic_plummer(n, W["seed"], 1.0))
         e0 = gb.energy(x0, n, eps, 1.0 / n)
-        mlp = load_mlp()
-        tols = [3e-12, 1e-11, 3e-11]
+        mlp = load_mlp(args.mlp)
+        tols = [float(t) for t in args.sweep_tols.split(",")]
         sweep = {}
         for ctl in ("reference", "pi", "learned"):
             integrate_once(gb, torch, x0, stream, "mixed", ctl, 1e-11, mlp)  # warm-up
@@ -735,7 +737,8 @@ def run_other_workload(args):
                 ms, st, xs = integrate_once(gb, torch, x0, stream, "mixed", ctl, tol, mlp)
                 rows.append({"tol": tol, **arm_record(gb, x0, e0, ms, st, xs)})
             sweep[ctl] = rows
-        target = float(np.exp(np.mean([np.log(sweep[c][1]["energy_rel_err"]) for c in sweep])))
+        mid = len(tols) // 2
+        target = float(np.exp(np.mean([np.log(sweep[c][mid]["energy_rel_err"]) for c in sweep])))
 
         def at_target(rows):
             le = np.log([r["energy_rel_err"] for r in rows])
@@ -755,7 +758,8 @@ def run_other_workload(args):
                     metric="time to tf at equal relative energy error (learned / PI / reference)",
                     dtype="f32+f64", steps=1, ms_per_step=1e3 * eq["learned"]["time_to_tf_s"],
                     energy_target=target, sweep=sweep, at_equal_energy=eq,
-                    config={**W, "tols": tols, "proposer": PROPOSER,
+                    config={**W, "tols": tols,
+                            "proposer": os.path.basename(args.mlp) if args.mlp else PROPOSER,
                             "step": "whole integrations, three tolerances per controller"})
     elif args.workload == "c1":
         n, eps, tol = 1024, 0.01, 1e-10

@@ -467,6 +467,11 @@ __global__ void batch_init_ctrl_kernel(const BatchParams P, const double* __rest
   c.pi_beta = pi_beta;
   c.pi_alpha = 1.0 / (1.0 + q) - 0.75 * pi_beta;
   c.err_prev = 1.0e-4;
+  {
+    // the learned proposer's tolerance feature (scalar tolerances per system)
+    const double ts = fmax(P.sys[k].atol, P.sys[k].rtol);
+    c.log_tol = ts > 0.0 ? log(ts) : 0.0;
+  }
   c.fsal = fsal;
   c.k0_valid = 1;
   c.n_rhs = 2;

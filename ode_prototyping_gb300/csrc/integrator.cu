@@ -800,7 +800,7 @@ __global__ void centroid_state_kernel(const double* __restrict__ x, long long n,
 __global__ void init_ctrl_kernel(Ctrl* C, const double* __restrict__ d, double t0, double tf,
                                  double* times_ring, int p, int q, double safety,
                                  int controller, double pi_beta, int fsal,
-                                 long long max_attempts, int exact) {
+                                 long long max_attempts, int exact, double log_tol) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const double d0 = d[0], d1 = d[1];
   const double dt0 = initial_dt0(d0, d1);
@@ -828,6 +828,7 @@ __global__ void init_ctrl_kernel(Ctrl* C, const double* __restrict__ d, double t
   c.pi_beta = pi_beta;
   c.pi_alpha = 1.0 / (1.0 + q) - 0.75 * pi_beta;
   c.err_prev = 1.0e-4;
+  c.log_tol = log_tol;
   c.fsal = fsal;
   c.k0_valid = 1;  // f(x0) computed for the estimate is k_0 of the first attempt
   c.k0slot = 0;
@@ -1502,9 +1503,13 @@ extern "C" int gb_integrator_start(gb_integrator it, const double* x0, double t0
   GB_CUDA_TRY(cudaGetLastError());
   const int q = it->htab.p < it->htab.pt ? it->htab.p : it->htab.pt;
   const double safety = std::pow(0.38, (1.0 / (1.0 + q)));
+  // the learned proposer's tolerance feature: scalar tolerances only
+  const double tol_scale = std::max(atol_s, rtol_s);
+  const double log_tol =
+      (atol_dev || rtol_dev || !(tol_scale > 0.0)) ? 0.0 : std::log(tol_scale);
   init_ctrl_kernel<<<1, 32, 0, s>>>(it->ctrl, d, t0, tf, it->times_ring, it->htab.p, q, safety,
                                     it->opts.controller, it->opts.pi_beta, it->tab.fsal,
-                                    it->opts.max_attempts, it->opts.exact);
+                                    it->opts.max_attempts, it->opts.exact, log_tol);
   GB_CUDA_TRY(cudaGetLastError());
   max_acc_kernel<<<1, 256, 0, s>>>(f0, n, it->ctrl);
   GB_CUDA_TRY(cudaGetLastError());

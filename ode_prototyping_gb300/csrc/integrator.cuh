@@ -20,6 +20,8 @@ struct Ctrl {
   double dt_hist[3];  // last three attempted step sizes
   double err_hist[3]; // last three error norms
   double learned_dt;  // last learned proposal
+  double log_tol;     // log max(atol, rtol) for scalar tolerances, 0 for vector ones
+                      // (the learned proposer's tolerance feature)
   long long n_accepted, n_rejected, n_attempts, n_rhs, n_rhs_saved;
   long long max_attempts;
   long long n_learned, n_learned_rejected;

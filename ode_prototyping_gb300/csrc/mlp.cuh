@@ -38,7 +38,12 @@ __device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x));
 //  10   log of the step relative to the integration interval
 //  11   1 if the last attempt was accepted
 //  12   log(dt_{n} / dt_{n-1})
-//  13-15 zero
+//  13   log of the PI memory (the last accepted error)
+//  14   log max(atol, rtol) (scalar tolerances; 0 for vector ones).  Networks
+//       trained at one tolerance saw a constant here and carry in_scale 0
+//       for it, so they ignore it; a network trained over several
+//       tolerances uses it.
+//  15   zero
 __device__ __forceinline__ void make_features(const Ctrl& c, const DevTableau& tab, long long n,
                                               float* f) {
   const double tiny = 1e-300;
@@ -56,7 +61,8 @@ __device__ __forceinline__ void make_features(const Ctrl& c, const DevTableau& t
   f[11] = (float)c.last_accepted;
   f[12] = (float)(log(fmax(c.dt_hist[0], tiny)) - log(fmax(c.dt_hist[1], tiny)));
   f[13] = (float)log(fmax(c.err_prev, 1e-30));  // PI memory: last accepted error
-  f[14] = f[15] = 0.f;
+  f[14] = (float)c.log_tol;  // log max(atol, rtol): one network for several tolerances
+  f[15] = 0.f;
 }
 
 // Single-thread BF16-weight / FP32-accumulate forward pass.

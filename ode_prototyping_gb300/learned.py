@@ -58,11 +58,17 @@ def member(n, softening, i: int):
     return int(nn), float(soft)
 
 
-def collect_logs(seeds, n: int, softening: float, tab: str, tol: float, tf: float,
+def tolerances(tol) -> list:
+    """A config's tolerance: one value, or a list (every seed is run at each)."""
+    return list(tol) if isinstance(tol, (list, tuple)) else [tol]
+
+
+def collect_logs(seeds, n: int, softening: float, tab: str, tol, tf: float,
                  attempts: int, precision: str = "mixed", controller: str = "reference",
                  mlp: GbMlp | None = None, ic: str = "plummer"):
     logs = []
-    for i, seed in enumerate(seeds):
+    runs = [(seed, t) for t in tolerances(tol) for seed in seeds]
+    for i, (seed, tol) in enumerate(runs):
         nn, soft = member(n, softening, i)
         x0 = initial_state(ic, nn, seed)
         exe = Gb300Executor(precision=precision, controller=controller, attempts_per_sync=16,
@@ -254,6 +260,12 @@ CONFIGS = {
     # controller, hence the multi-size configuration below)
     "plummer512_dopri5_tol1e-9": dict(ic="plummer", n=512, softening=0.005, tab="DOPRI5",
                                       tol=1e-9, tf=1.0, attempts=600),
+    # the single large system over tolerances 1e-8 .. 1e-12: one network for
+    # all of them, with log max(atol, rtol) as a feature (every seed of the set
+    # is run at each tolerance)
+    "plummer16384_rkf78_multitol": dict(ic="plummer", n=16384, softening=0.005, tab="RKF78",
+                                        tol=[1e-8, 1e-9, 1e-10, 1e-11, 1e-12], tf=2.0,
+                                        attempts=1200),
     # configuration 3's members: Plummer spheres with virial ratio in [0.5, 1.5),
     # N cycling through 64 .. 4096 (log-spaced), eps = 0.01 * 4 / N^(1/3),
     # DOPRI5, tol 1e-9, t in [0, 1] (the proposer the batched C3 workload runs)
@@ -270,11 +282,16 @@ def train_config(name: str, seeds=None, rounds: int = 3, rho: float = 0.38, epoc
                c["attempts"], rounds=rounds, rho=rho, epochs=epochs, ic=c["ic"])
 
 
-def evaluate_config(name: str, mlp: GbMlp, seeds=None) -> dict:
+def evaluate_config(name: str, mlp: GbMlp, seeds=None, tol=None) -> dict:
     """Reference, PI and learned controllers on held-out seeds, plus the
-    learned run's gain over the reference controller."""
+    learned run's gain over the reference controller.  A config with several
+    tolerances is evaluated at each (a dict keyed by tolerance) unless tol
+    picks one."""
     c = CONFIGS[name]
-    ev = evaluate(c["n"], c["softening"], c["tab"], c["tol"], c["tf"], seeds or SEEDS_B[:4], mlp,
+    tols = tolerances(c["tol"]) if tol is None else [tol]
+    if len(tols) > 1:
+        return {f"{t:g}": evaluate_config(name, mlp, seeds, t) for t in tols}
+    ev = evaluate(c["n"], c["softening"], c["tab"], tols[0], c["tf"], seeds or SEEDS_B[:4], mlp,
                   ic=c["ic"])
     states = {k: v.pop("states") for k, v in ev.items()}
     ref, lrn = ev["reference"], ev["learned"]
@@ -300,12 +317,13 @@ def main(argv=None):
     ap.add_argument("--rho", type=float, default=0.38)
     ap.add_argument("--rounds", type=int, default=3)
     ap.add_argument("--seeds", type=int, default=8, help="seeds 1..k of seed set A")
+    ap.add_argument("--eval-seeds", type=int, default=4, help="seeds of seed set B evaluated")
     a = ap.parse_args(argv)
     t0 = time.time()
     m, info = train_config(a.config, SEEDS_A[:a.seeds], rounds=a.rounds, rho=a.rho)
     with open(a.out, "wb") as f:
         f.write(bytes(m))
-    ev = evaluate_config(a.config, m)
+    ev = evaluate_config(a.config, m, SEEDS_B[:a.eval_seeds])
     print(json.dumps({"config": a.config, "train": info, "train_s": time.time() - t0,
                       "evaluation": ev}, indent=1))
 

@@ -87,3 +87,20 @@ def test_shipped_weights_match_the_struct_and_a_configuration():
         assert np.all(np.isfinite(flat)), name
         assert all(s >= 0 for s in m.in_scale) and any(s > 0 for s in m.in_scale), name
         assert m.out_scale > 0, name
+
+
+def test_shipped_single_tolerance_proposers_ignore_the_tolerance_feature(gb):
+    """Proposers trained at one tolerance saw a constant feature 14 (log max
+    of the tolerances) and carry a zero input scale for it; the
+    multi-tolerance proposer uses it."""
+    import glob
+    import os
+    wdir = os.path.join(os.path.dirname(gb.__file__), "weights")
+    paths = sorted(glob.glob(os.path.join(wdir, "*.bin")))
+    assert paths
+    for path in paths:
+        m = gb.GbMlp.from_buffer_copy(open(path, "rb").read())
+        if "multitol" in os.path.basename(path):
+            assert m.in_scale[14] > 0.0, path
+        else:
+            assert m.in_scale[14] == 0.0, path
