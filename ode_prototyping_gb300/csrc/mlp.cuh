@@ -106,6 +106,9 @@ __device__ __forceinline__ void mlp_infer_block(const void* mlp_v, const float* 
   float contrib = 0.f;
   if (o < kHid) {
     float acc = M->b2[o];
+    // unrolled so that the row's weight loads are in flight together (the
+    // sum keeps its order)
+#pragma unroll
     for (int k = 0; k < kHid; ++k) acc = fmaf(__bfloat162float(M->w2[o * kHid + k]), h1[k], acc);
     contrib = __bfloat162float(M->w3[o]) * silu(acc);
   }
@@ -145,6 +148,7 @@ __device__ __forceinline__ float mlp_infer_warp(const void* mlp_v, const float* 
   for (int r = 0; r < 2; ++r) {
     const int u = lane + 32 * r;
     float acc = M->b2[u];
+#pragma unroll
     for (int k = 0; k < kHid; ++k) {
       const float hk = __shfl_sync(0xffffffffu, k < 32 ? h1[0] : h1[1], k & 31);
       acc = fmaf(__bfloat162float(M->w2[u * kHid + k]), hk, acc);
