@@ -860,14 +860,19 @@ def run_other_workload(args):
                  "energy_rel_err_max": float(np.max(errs))}
             print(json.dumps({"arm": [prec, ctl], **r}), flush=True)
             return r
-        ctls = ["reference", "pi"] + (["learned"] if mlp is not None else [])
+        # --no-fp64: the mixed arm with the reference controller only (a short
+        # run, e.g. for profiling the stage kernel)
+        ctls = ["reference"] + ([] if args.no_fp64 else
+                                ["pi"] + (["learned"] if mlp is not None else []))
         arms = {f"mixed_{c}": run_arm("mixed", c, args.steps) for c in ctls}
-        arms["f64_reference"] = run_arm("f64", "reference", 1)
-        f64 = arms["f64_reference"]
-        for key in [k for k in arms if k != "f64_reference"]:
-            arms[f"speedup_time_to_tf_{key}_vs_f64"] = f64["time_to_tf_s"] / arms[key]["time_to_tf_s"]
-            arms[f"speedup_accepted_steps_per_s_{key}_vs_f64"] = (
-                arms[key]["accepted_steps_per_s"] / f64["accepted_steps_per_s"])
+        if not args.no_fp64:
+            arms["f64_reference"] = run_arm("f64", "reference", 1)
+            f64 = arms["f64_reference"]
+            for key in [k for k in arms if k != "f64_reference"]:
+                arms[f"speedup_time_to_tf_{key}_vs_f64"] = (f64["time_to_tf_s"]
+                                                            / arms[key]["time_to_tf_s"])
+                arms[f"speedup_accepted_steps_per_s_{key}_vs_f64"] = (
+                    arms[key]["accepted_steps_per_s"] / f64["accepted_steps_per_s"])
         head = arms.get("mixed_learned", arms["mixed_reference"])
         line.update(value=head["accepted_steps_per_s"], dtype="f32+f64",
                     steps=args.steps, ms_per_step=1e3 * head["time_to_tf_s"],
