@@ -312,8 +312,8 @@ typedef struct {
   int32_t log_steps;          /* record per-attempt controller logs on the device */
   int32_t spatial_sort;       /* mixed precision: 0 = default (uniform masses, N >= 8192:
                                  the partner-chunk stage on Morton-sorted bodies, where
-                                 half tiles whose boxes are far from the i-tile skip the
-                                 close-pair test), 1 = Morton-sorted tiles with the
+                                 64-partner quarter tiles whose boxes are far from every
+                                 body of a warp skip the close-pair test), 1 = Morton-sorted tiles with the
                                  tile-centroid far-field path, 2 = the sorted chunk stage
                                  without that culling (the same bits as 0), 3 = the
                                  chunk stage in body order */

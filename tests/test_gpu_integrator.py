@@ -161,8 +161,8 @@ def _mixed_run(gb, ode, x0, tf, tol, tile=None, variant=0, spatial_sort=0, tab="
 @pytest.mark.parametrize("n,gen", [(16384, "plummer"), (8333, "cold"), (12000, "binary")])
 def test_split_stage_tile_culling_is_bit_identical(gb, torch_cuda, n, gen):
     """The partner-chunk stage on Morton-sorted bodies skips the close-pair
-    test for half tiles whose boxes are far from the i-tile; the terms it adds
-    there are the ones the test would have kept, so whole RKF78 trajectories
+    test for 64-partner quarter tiles whose boxes are far from every body of a
+    warp; the terms it adds there are the ones the test would have kept, so whole RKF78 trajectories
     with and without the culling (re-sorted every 4 attempts) agree bit for
     bit, and both follow the FP64 integration to the mixed-precision bound."""
     x0 = {"plummer": lambda: gb.ic_plummer(n, 5), "cold": lambda: gb.ic_cold_sphere(n, 6, 0.01),
