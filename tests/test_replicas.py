@@ -90,3 +90,17 @@ def test_conservation_drift():
     assert abs(d["energy_rel_err"] - 2e-9) < 1e-15
     assert abs(d["momentum_drift"] - 5e-12) < 1e-20
     assert abs(d["angular_momentum_drift"] - 1e-11) < 1e-16
+
+
+def test_pipe_probe_compiles(tmp_path):
+    """The throughput probe behind `bench.py --workload pipes` builds for
+    sm_103a (nvcc cross-compiles without a GPU); running it needs one."""
+    import shutil
+    import subprocess
+    nvcc = "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") \
+        else shutil.which("nvcc")
+    if nvcc is None:
+        pytest.skip("nvcc not found")
+    src = os.path.join(ROOT, "ode_prototyping_gb300", "csrc", "probe", "pipes.cu")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                    "-c", src, "-o", str(tmp_path / "pipes.o")], check=True)
