@@ -586,6 +586,21 @@ def main():
                      "fp32_pipe_cap_frac": FLOPS_PER_INTERACTION / 2 / HILO_FP32_OPS},
     }
     if rank == 0:
+        # the measured ceilings the roofline fraction is read against
+        try:
+            pp = pipe_probe()
+            line["roofline"]["measured_ceilings"] = {
+                "f32x2_fma_frac_of_nominal": pp["ffma2_frac"],
+                "scalar_fma_frac_of_nominal": pp["ffma_frac"],
+                "sfu_rsqrt_per_sm_per_clock": pp["rsqrt_per_sm_per_clock"],
+                "pair_loop_alone_frac_20flop": pp["pair_loop_frac_20flop"],
+                "kernel_frac_of_pair_loop_ceiling": line["roofline"]["frac"]
+                / pp["pair_loop_frac_20flop"],
+                "note": "ode_prototyping_gb300/csrc/probe/pipes.cu: independent FMA chains, "
+                        "and the stage kernel's pair loop without the close-pair test, "
+                        "barriers, tails or epilogue (records in shared memory)"}
+        except Exception as ex:  # reported, not fatal
+            line["roofline"]["measured_ceilings"] = {"error": repr(ex)}
         line["e2e"] = e2e(gb, torch, x0, mlp)
         line["mixed_accuracy"] = mixed_accuracy(gb, x0_dev, n, eps)
         line["config2_tol_1e-8"] = config2_tolerance(gb, torch, x0_dev, e0)
@@ -634,18 +649,24 @@ def _batch_ics(gb, torch, sizes, seeds, kind, eps):
     return np.concatenate(xs)
 
 
-def run_pipe_probe():
-    """Throughput ceilings for the force kernel's roofline: builds and runs
-    ode_prototyping_gb300/csrc/probe/pipes.cu (scalar and f32x2 FMA, SFU
-    rsqrt, the pair loop alone) and prints its JSON line."""
+def pipe_probe() -> dict:
+    """Throughput ceilings for the force kernel's roofline: runs
+    ode_prototyping_gb300/csrc/probe/pipes.cu (built by the library build;
+    compiled here if missing) -- scalar and f32x2 FMA, SFU rsqrt, and the
+    pair loop alone -- and returns its measurements."""
     src = os.path.join(ROOT, "ode_prototyping_gb300", "csrc", "probe", "pipes.cu")
     exe = os.path.join(ROOT, "ode_prototyping_gb300", "_build", "probe_pipes")
-    os.makedirs(os.path.dirname(exe), exist_ok=True)
-    nvcc = "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc"
-    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", src,
-                    "-o", exe], check=True)
+    if not os.path.exists(exe) or os.path.getmtime(exe) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(exe), exist_ok=True)
+        nvcc = "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc"
+        subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                        src, "-o", exe], check=True)
     r = subprocess.run([exe], check=True, capture_output=True, text=True)
-    print(json.dumps({"workload": "pipes", **json.loads(r.stdout)}), flush=True)
+    return json.loads(r.stdout)
+
+
+def run_pipe_probe():
+    print(json.dumps({"workload": "pipes", **pipe_probe()}), flush=True)
 
 
 def run_other_workload(args):

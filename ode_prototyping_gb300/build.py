@@ -20,6 +20,10 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(BUILD, "libgbode.so")
+# throughput probe of the force kernel's roofline (a standalone program, not
+# part of the library; bench.py --workload pipes and the headline line run it)
+PROBE_SRC = os.path.join(CSRC, "probe", "pipes.cu")
+PROBE = os.path.join(BUILD, "probe_pipes")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -63,6 +67,8 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
             if ptxas_info:
                 cmd += ["-Xptxas", "-v"]
             jobs.append((s, cmd))
+    if os.path.exists(PROBE_SRC) and (force or _stale(PROBE, [PROBE_SRC])):
+        jobs.append(("probe/pipes.cu", [cc, *ARCH, "-O3", "-std=c++17", PROBE_SRC, "-o", PROBE]))
     outputs = {}
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         futs = {ex.submit(subprocess.run, cmd, capture_output=True, text=True): s for s, cmd in jobs}
@@ -75,7 +81,8 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
             if verbose or ptxas_info:
                 sys.stderr.write(f"== {futs[f]}\n{r.stderr}")
     objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in srcs]
-    if force or jobs or _stale(LIB, objs):
+    if force or any(name.endswith(".cu") and "/" not in name for name, _ in jobs) or \
+            _stale(LIB, objs):
         cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fPIC"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
