@@ -83,15 +83,18 @@ def _zero_mlp(gb):
     return m
 
 
-def test_batch_learned_controller(gb, torch_cuda):
+@pytest.mark.parametrize("spc", [1, 2])
+def test_batch_learned_controller(gb, torch_cuda, spc):
     """The batched control warp evaluates the proposer per system; with a
     zero-output network every system takes the same accepted steps as the
-    single-system integrator under the same network."""
+    single-system integrator under the same network, with one system per CTA
+    or with the small ones sharing a CTA."""
     sizes = [48, 96, 160]
     soft, tol, tf = 0.05, 1e-9, 0.1
     xs, x0 = _systems(gb, sizes, 70)
     m = _zero_mlp(gb)
-    b = gb.Batch("DOPRI5", sizes, soft, precision="f64", controller="learned", mlp=m)
+    b = gb.Batch("DOPRI5", sizes, soft, precision="f64", controller="learned", mlp=m,
+                 tiling=gb.GbBatchTiling(128, 1, 1, 0, spc))
     b.start(x0, 0.0, tf, tol, tol)
     assert b.advance() == 0
     st = b.stats(per_system=True)
