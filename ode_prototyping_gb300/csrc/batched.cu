@@ -480,6 +480,7 @@ __global__ void batch_init_ctrl_kernel(const BatchParams P, const double* __rest
     c.dt_hist[h] = c.dt;
     c.err_hist[h] = 1.0;
   }
+  init_log_cache(c, P.sys[k].n);
   c.done = (c.t < c.tf) ? 0 : 1;
   P.ctrl[k] = c;
   if (c.done) atomicAdd(P.n_done, 1u);

@@ -66,6 +66,20 @@ struct CtrlEnv {
   long long n;           // bodies
 };
 
+// Fills the learned controller's log caches from the histories (at start;
+// other controllers leave them unused).
+__device__ __forceinline__ void init_log_cache(Ctrl& c, long long n) {
+  c.lg_valid = c.controller == GB_CTRL_LEARNED;
+  if (!c.lg_valid) return;
+  for (int k = 0; k < 3; ++k) {
+    c.lg_dt[k] = log(fmax(c.dt_hist[k], 1e-300));
+    c.lg_err[k] = log(fmax(c.err_hist[k], 1e-30));
+  }
+  c.lg_err_prev = log(fmax(c.err_prev, 1e-30));
+  c.lg_safety = log(c.safety);
+  c.lg_n = log((double)n);
+}
+
 // Shifts the step/error history as finish_attempt will (used to build the
 // learned controller's features before the decision is applied).
 __device__ __forceinline__ void preview_history(Ctrl& c, double err, bool accepted) {
@@ -76,6 +90,14 @@ __device__ __forceinline__ void preview_history(Ctrl& c, double err, bool accept
   c.dt_hist[0] = c.dt;
   c.err_hist[0] = isfinite(err) ? err : 1e300;
   c.last_accepted = accepted ? 1 : 0;
+  if (c.lg_valid) {
+    for (int k = 2; k > 0; --k) {
+      c.lg_dt[k] = c.lg_dt[k - 1];
+      c.lg_err[k] = c.lg_err[k - 1];
+    }
+    c.lg_dt[0] = log(fmax(c.dt_hist[0], 1e-300));
+    c.lg_err[0] = log(fmax(c.err_hist[0], 1e-30));
+  }
 }
 
 // End-of-attempt decision by one thread: acceptance (err <= 1,
@@ -139,8 +161,11 @@ __device__ inline void finish_attempt(const DevTableau& tab, const CtrlEnv& P, C
       // ratio log(safety) - alpha log(err) + beta log(err_prev) (a network
       // that has learned nothing reproduces PI); the embedded error
       // estimate of the next attempt still decides acceptance.
-      const double base = err > 0.0 ? log(c.safety) - c.pi_alpha * log(err) +
-                                          c.pi_beta * log(c.err_prev)
+      // log(err) is the cached log fmax(err, 1e-30) when err >= 1e-30 (the
+      // same value); log(err_prev) is the cached one (err_prev >= 1e-4)
+      const double lerr = err >= 1e-30 ? c.lg_err[0] : log(err);
+      const double base = err > 0.0 ? c.lg_safety - c.pi_alpha * lerr +
+                                          c.pi_beta * c.lg_err_prev
                                     : log(kMaxStepScale);
       const double res = fmin(fmax(learned_log_scale, -kLearnedMaxLogCorrection),
                               kLearnedMaxLogCorrection);
@@ -153,9 +178,11 @@ __device__ inline void finish_attempt(const DevTableau& tab, const CtrlEnv& P, C
       c.learned_active = 1;
       // keep the PI memory current
       c.err_prev = fmax(err, 1.0e-4);
+      c.lg_err_prev = err >= 1.0e-4 ? lerr : log(fmax(c.err_prev, 1e-30));
       c.reject_prev = 0;
     } else {
       dtn = pi_step(c, dt, err, accepted);  // fallback on every rejection
+      if (accepted && c.lg_valid) c.lg_err_prev = log(fmax(c.err_prev, 1e-30));
     }
   } else {
     dtn = reference_step(dt, err, c.safety, c.q, c.t0, c.tf, c.exact_pow != 0);

@@ -800,7 +800,8 @@ __global__ void centroid_state_kernel(const double* __restrict__ x, long long n,
 __global__ void init_ctrl_kernel(Ctrl* C, const double* __restrict__ d, double t0, double tf,
                                  double* times_ring, int p, int q, double safety,
                                  int controller, double pi_beta, int fsal,
-                                 long long max_attempts, int exact, double log_tol) {
+                                 long long max_attempts, int exact, double log_tol,
+                                 long long n) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const double d0 = d[0], d1 = d[1];
   const double dt0 = initial_dt0(d0, d1);
@@ -840,6 +841,7 @@ __global__ void init_ctrl_kernel(Ctrl* C, const double* __restrict__ d, double t
     c.dt_hist[k] = c.dt;
     c.err_hist[k] = 1.0;
   }
+  init_log_cache(c, n);
   c.done = (t0 < tf) ? 0 : 1;
   times_ring[0] = t0;
   *C = c;
@@ -1509,7 +1511,7 @@ extern "C" int gb_integrator_start(gb_integrator it, const double* x0, double t0
       (atol_dev || rtol_dev || !(tol_scale > 0.0)) ? 0.0 : std::log(tol_scale);
   init_ctrl_kernel<<<1, 32, 0, s>>>(it->ctrl, d, t0, tf, it->times_ring, it->htab.p, q, safety,
                                     it->opts.controller, it->opts.pi_beta, it->tab.fsal,
-                                    it->opts.max_attempts, it->opts.exact, log_tol);
+                                    it->opts.max_attempts, it->opts.exact, log_tol, n);
   GB_CUDA_TRY(cudaGetLastError());
   max_acc_kernel<<<1, 256, 0, s>>>(f0, n, it->ctrl);
   GB_CUDA_TRY(cudaGetLastError());

@@ -22,6 +22,16 @@ struct Ctrl {
   double learned_dt;  // last learned proposal
   double log_tol;     // log max(atol, rtol) for scalar tolerances, 0 for vector ones
                       // (the learned proposer's tolerance feature)
+  // Logs the learned controller reuses from attempt to attempt (lg_valid):
+  // each is the same log call on the same argument as the value it stands
+  // for, so features and proposals keep their bits while the one controller
+  // thread evaluates far fewer FP64 logs per attempt.
+  double lg_dt[3];    // log fmax(dt_hist[k], 1e-300)
+  double lg_err[3];   // log fmax(err_hist[k], 1e-30)
+  double lg_err_prev; // log fmax(err_prev, 1e-30)
+  double lg_safety;   // log safety
+  double lg_n;        // log N
+  int lg_valid;
   long long n_accepted, n_rejected, n_attempts, n_rhs, n_rhs_saved;
   long long max_attempts;
   long long n_learned, n_learned_rejected;

@@ -47,20 +47,38 @@ __device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x));
 __device__ __forceinline__ void make_features(const Ctrl& c, const DevTableau& tab, long long n,
                                               float* f) {
   const double tiny = 1e-300;
+  // the learned controller keeps these logs from attempt to attempt
+  // (Ctrl::lg_*, the same values); a log of another controller computes them
+  double ldt[3], lerr[3], lprev, ln;
+  if (c.lg_valid) {
+    for (int k = 0; k < 3; ++k) {
+      ldt[k] = c.lg_dt[k];
+      lerr[k] = c.lg_err[k];
+    }
+    lprev = c.lg_err_prev;
+    ln = c.lg_n;
+  } else {
+    for (int k = 0; k < 3; ++k) {
+      ldt[k] = log(fmax(c.dt_hist[k], tiny));
+      lerr[k] = log(fmax(c.err_hist[k], 1e-30));
+    }
+    lprev = log(fmax(c.err_prev, 1e-30));
+    ln = log((double)n);
+  }
   for (int k = 0; k < 3; ++k) {
-    f[k] = (float)log(fmax(c.dt_hist[k], tiny));
-    f[3 + k] = (float)log(fmax(c.err_hist[k], 1e-30));
+    f[k] = (float)ldt[k];
+    f[3 + k] = (float)lerr[k];
   }
   const double amax = fmax(c.max_abs_acc, 1e-30);
   f[6] = (float)log(amax);
   const double m = 1.0 / (double)n;
   f[7] = (float)(0.5 * log(m / amax));
-  f[8] = (float)log((double)n);
+  f[8] = (float)ln;
   f[9] = (float)(tab.p < tab.pt ? tab.p : tab.pt);
   f[10] = (float)log(fmax(c.dt_hist[0] / fmax(c.tf - c.t0, tiny), tiny));
   f[11] = (float)c.last_accepted;
-  f[12] = (float)(log(fmax(c.dt_hist[0], tiny)) - log(fmax(c.dt_hist[1], tiny)));
-  f[13] = (float)log(fmax(c.err_prev, 1e-30));  // PI memory: last accepted error
+  f[12] = (float)(ldt[0] - ldt[1]);
+  f[13] = (float)lprev;  // PI memory: last accepted error
   f[14] = (float)c.log_tol;  // log max(atol, rtol): one network for several tolerances
   f[15] = 0.f;
 }
